@@ -1,0 +1,282 @@
+/*
+ * meso_gpu.h -- C ABI of the GB300 DUGKS / CDUGKS / Shakhov step library.
+ *
+ * A drop-in for the step loop of meso-lts (src/meso/exec.cpp:81-165): the
+ * host keeps the case file, the Gambit meshes and the output formats, and
+ * every call below replaces one member of the reference solver classes
+ * (include/solver/boltzmann/{dugks,cdugks,cdugks_shakhov}.h).  Plain C types
+ * only: pointers, sizes and the descriptor structs declared here.
+ *
+ * Conventions
+ *   - Every function returns MESO_OK (0) or one MESO_ERR_* code; the message
+ *     of the last failure on the calling thread is meso_last_error().
+ *     No C++ exception crosses this boundary.
+ *   - All arrays are caller-owned host memory, indexed in the ORIGINAL order
+ *     of the .neu file (cells and faces as the reference numbers them); the
+ *     library renumbers internally (reverse Cuthill-McKee cells, faces sorted
+ *     by owner) and maps back on every read.
+ *   - One context per host thread at a time (contexts are not internally
+ *     locked); each context owns one CUDA stream on the current device.
+ *   - Vectors are xyz triples, 3 doubles per entry, also in 2D (z = 0).
+ */
+#ifndef MESO_GPU_H
+#define MESO_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MESO_OK 0
+#define MESO_ERR_INVALID 1     /* bad argument or descriptor (std::invalid_argument in the reference) */
+#define MESO_ERR_CUDA 2        /* CUDA runtime failure, or no usable GPU */
+#define MESO_ERR_OOM 3         /* device allocation failed */
+#define MESO_ERR_NAN 4         /* a cell produced rho = NaN or T < 0 with no mask (run_state = false) */
+#define MESO_ERR_TIMEOUT 5     /* a bounded device wait gave up */
+#define MESO_ERR_IO 6          /* case, mesh or DVS file missing or malformed */
+#define MESO_ERR_UNSUPPORTED 7 /* valid input that this build does not implement */
+#define MESO_ERR_CAPACITY 8    /* request larger than a fixed capacity */
+
+/* ---- solver kinds: the dispatch strings of src/meso/main.cpp:49-54 ------- */
+#define MESO_SOLVER_DUGKS 0          /* "dugks@incompressible"  (class DUGKS)          */
+#define MESO_SOLVER_CDUGKS 1         /* "cdugks@incompressible" (class CDUGKS)         */
+#define MESO_SOLVER_CDUGKS_SHAKHOV 2 /* "cdugks@shakhov"        (class CDUGKS_SHAKHOV) */
+
+/* ---- storage precision of the distribution functions -------------------- */
+#define MESO_FP64 0 /* plain form: f, face values and fluxes in FP64 (parity form)            */
+#define MESO_FP32 1 /* f stored and streamed in FP32; moments, equilibria, wall sums in FP64 */
+
+/* ---- boundary types: BoundaryType of include/solver/config.h:13-23 ------- */
+#define MESO_BC_FLUID_INTERIOR 0
+#define MESO_BC_FARFIELD_INLET 1
+#define MESO_BC_PRESSURE_INLET 2
+#define MESO_BC_FREESTREAM_INLET 3
+#define MESO_BC_FARFIELD_OUTLET 4
+#define MESO_BC_PRESSURE_OUTLET 5
+#define MESO_BC_WALL 6
+#define MESO_BC_SLIP_WALL 7
+#define MESO_BC_SYMMETRY 8
+
+/* ---- patch value types: PatchType of include/solver/config.h:25-36 ------ */
+#define MESO_PATCH_ZERO_GRADIENT 0
+#define MESO_PATCH_FIXED_VALUE 1
+#define MESO_PATCH_CALCULATED 2
+#define MESO_PATCH_FROM_FILE 3
+#define MESO_PATCH_SWITCH 4
+
+/*
+ * Physical mesh, flattened from fvmMesh::Mesh (include/mesh/object.h:93-179)
+ * after Mesh::build_geom (src/mesh/object.cpp:94-172).  CSR lists keep the
+ * reference's per-cell order: Cell::face_id (local face order) and
+ * Cell::neighbors (first-seen order over the cell's faces).
+ */
+typedef struct meso_mesh_desc {
+    int32_t dim;                 /* 2 or 3 (Mesh::NDFVL) */
+    int32_t ncell, nface;
+    const double *cell_pos;      /* [ncell*3] Cell::position              */
+    const double *cell_vol;      /* [ncell]   Cell::volume                */
+    const int32_t *cell_group;   /* [ncell]   Cell::group_id (index into groups) */
+    const int32_t *cell_face_ptr;/* [ncell+1] CSR into cell_face          */
+    const int32_t *cell_face;    /* Cell::face_id                         */
+    const int32_t *cell_nbr_ptr; /* [ncell+1] CSR into cell_nbr, lsq_w, lsq_dr */
+    const int32_t *cell_nbr;     /* Cell::neighbors                       */
+    const double *lsq_w;         /* LeastSquare::weight                   */
+    const double *lsq_dr;        /* LeastSquare::dr, 3 per entry          */
+    const double *lsq_c;         /* [ncell*9] LeastSquare::Cx, Cy, Cz     */
+    const int32_t *face_cell;    /* [nface*2] Face::cell_id {own, nei}; boundary faces {c, c} */
+    const double *face_pos;      /* [nface*3] Face::position              */
+    const double *face_area;     /* [nface]   Face::area                  */
+    const double *face_normal;   /* [nface*3] Face::normal_vector[0] (outward from own; [1] = -[0]) */
+    const int32_t *face_mark;    /* [nface]   index into the mark table (0 = fluid-interior) */
+    double min_cell_size;        /* Mesh::min_cell_size */
+    double total_volume;         /* Mesh::total_volume  */
+} meso_mesh_desc;
+
+/*
+ * Discrete velocity set, flattened from the DVS Mesh of
+ * src/solver/dvs/dvs_generator.cpp (position = xi, volume = weight,
+ * symmetry.id = mirror indices).  tensor_n > 0 declares a tensor-product set
+ * (Gauss-Hermite, half-range GH, Newton-Cotes) with index i + j*n (+ k*n*n)
+ * over the 1-D abscissae `axis`; 0 for Sparse or Gambit velocity meshes.
+ */
+typedef struct meso_dvs_desc {
+    int32_t nv;
+    const double *xi;            /* [nv*3] */
+    const double *w;             /* [nv]   */
+    const int32_t *sym;          /* [nv*3] Symmetry::id, may be NULL (all 0) */
+    int32_t tensor_n;
+    const double *axis;          /* [tensor_n] or NULL */
+    double max_magnitude;        /* Mesh::max_cell_magnitude of the DVS */
+} meso_dvs_desc;
+
+/*
+ * One face group ([mark] block of the case file, Mark/Patch of
+ * include/solver/config.h:38-114).  Missing patch keys take the reference's
+ * defaults (src/solver/boundary/patch.cpp:55-85): type 0, scalars 0,
+ * vectors 0.
+ */
+typedef struct meso_mark_desc {
+    int32_t type;                /* MESO_BC_* */
+    int32_t temperature_type;    /* PatchType of "temperature" (wall balance, cdugks_shakhov.cpp:473-479) */
+    int32_t direction;           /* "direction" objectType (symmetry, slip-wall) */
+    int32_t pad_;
+    double density;              /* "density"     */
+    double temperature;          /* "temperature" */
+    double pressure;             /* "pressure"    */
+    double velocity[3];          /* "velocity"    */
+    double alpha_u, alpha_T;     /* "slip-wall-alpha-u", "slip-wall-alpha-T" */
+} meso_mark_desc;
+
+/*
+ * Solver settings ([settings] of the case file).  The fields each solver
+ * reads are the ones its constructor / update_config reads:
+ *   CDUGKS  cdugks.cpp:7-15, 41-47;  DUGKS dugks.cpp:7-15, 41-48;
+ *   CDUGKS_SHAKHOV cdugks_shakhov.cpp:7-33.
+ */
+typedef struct meso_params {
+    int32_t solver;              /* MESO_SOLVER_* */
+    int32_t precision;           /* MESO_FP64 or MESO_FP32 */
+    int32_t gradient_switch;     /* "gradient-switch" */
+    int32_t limiter_switch;      /* "limiter-switch" (Shakhov) */
+    int32_t K;                   /* "gas-k" (Shakhov, integer as in the reference) */
+    int32_t residual_interval;   /* 100 in the reference (solver.h:49); 0 disables the check */
+    double dt;                   /* "timeStep" (DUGKS: derived from CFL in initial) */
+    double R;                    /* "gas-constant" */
+    double T0;                   /* "ref-temperature" */
+    double rho0, L0;             /* "ref-density", "ref-length" */
+    double mu0;                  /* "ref-viscosity" (Shakhov) */
+    double vhs_index;            /* "vhs-index" (Shakhov) */
+    double Pr;                   /* "Pr" (Shakhov) */
+    double Ma, Re;               /* "Ma", "Re" (BGK) */
+    double CFL;                  /* "CFL" (DUGKS) */
+    double venkata_k;            /* "venkata-limiter-k" */
+    double residual_limit;       /* "residual-limit" */
+} meso_params;
+
+/* Step state, the reference's run_state / step / solution_time plus the monitor of cdugks_shakhov.cpp:697-719. */
+typedef struct meso_status {
+    int32_t step;
+    int32_t run_state;           /* 1 while running; 0 after convergence or an unmasked NaN/T<0 */
+    int32_t converged;           /* 1 if run_state turned 0 by convergence */
+    int32_t bad_cells;           /* cells flagged by the last step's monitor */
+    int32_t first_bad_cell;      /* original-order id of the first flagged cell, -1 if none */
+    int32_t masked_repairs;      /* cumulative mask repairs (cell_value_interp) */
+    double solution_time;
+    double residual[8];          /* last residuals, in the reference's print order */
+    int32_t nresidual;
+    int32_t pad_;
+} meso_status;
+
+typedef struct meso_ctx meso_ctx;
+typedef struct meso_case meso_case;
+typedef struct meso_batch meso_batch;
+
+/* Message of the last failure on this thread ("" if none). */
+const char *meso_last_error(void);
+
+/* Library build information: "<version> sm_103a <build flags>". */
+const char *meso_version(void);
+
+/* ---- host-only case loading (no GPU needed) ----------------------------- */
+
+/*
+ * Parse a case file and build everything the reference constructor builds:
+ * Config (src/solver/config.cpp:18-108), the Gambit mesh and its geometry
+ * (src/mesh/mesh.cpp:4-11, object.cpp:38-172, geom.cpp), the DVS
+ * (dvs_generator.cpp), the solver settings (ctor / update_config) and the
+ * initial macroscopic fields from the [group] patches (initial(), e.g.
+ * cdugks_shakhov.cpp:103-132).  Relative paths resolve against the case
+ * file's directory.
+ */
+int meso_case_load(const char *case_file, meso_case **out);
+void meso_case_free(meso_case *c);
+/* Views into the loaded case; valid until meso_case_free. */
+int meso_case_mesh(const meso_case *c, meso_mesh_desc *mesh);
+int meso_case_dvs(const meso_case *c, meso_dvs_desc *dvs);
+int meso_case_marks(const meso_case *c, const meso_mark_desc **marks, int32_t *nmarks);
+int meso_case_params(const meso_case *c, meso_params *params);
+/* Patch values per cell from the [group] blocks (density/velocity/temperature, fixedValue or fromFile).
+ * mask[c] = the group's "mask" switch.  Any pointer may be NULL. */
+int meso_case_initial_fields(const meso_case *c, double *rho, double *u, double *T, uint8_t *mask);
+/* Settings that drive the step loop: max-step, write-interval, read-np-data, output-latest, output-np. */
+int meso_case_loop_settings(const meso_case *c, int32_t *max_step, int32_t *write_interval,
+                            int32_t *read_np_data, int32_t *output_latest, int32_t *output_np);
+
+/* ---- single solve ------------------------------------------------------- */
+
+/*
+ * Create a solver context on the current CUDA device from flat descriptors.
+ * Replaces the reference constructors (cdugks.cpp:7-39, dugks.cpp:7-39,
+ * cdugks_shakhov.cpp:35-60) after the mesh and DVS are built.  mask may be
+ * NULL (no cell is masked, cdugks_shakhov.cpp:701-707).
+ */
+int meso_ctx_create(const meso_mesh_desc *mesh, const meso_dvs_desc *dvs, const meso_mark_desc *marks,
+                    int32_t nmarks, const meso_params *params, const uint8_t *mask, meso_ctx **out);
+
+/* Same from a case file: meso_case_load + meso_ctx_create, precision overriding the file's. */
+int meso_ctx_create_from_case(const char *case_file, int32_t precision, meso_ctx **out);
+
+void meso_ctx_destroy(meso_ctx *ctx);
+
+/*
+ * initial(): equilibrium state from macroscopic fields.
+ *   mode 0 -- group-patch path (cdugks.cpp:66-105, cdugks_shakhov.cpp:102-169):
+ *             f = equilibrium(rho, u, T); the stored macros are then the
+ *             discrete moments of f.  q is ignored.
+ *   mode 1 -- read-np-data path (cdugks.cpp:56-65, cdugks_shakhov.cpp:81-101):
+ *             f = Maxwell / Shakhov(rho, u, T, q); the macros are kept as given.
+ * T and q are ignored by the BGK solvers and may be NULL there.
+ */
+int meso_init_macros(meso_ctx *ctx, const double *rho, const double *u, const double *T, const double *q,
+                     int32_t mode);
+
+/* initial() for a context made by meso_ctx_create_from_case: the case's own groups / read-np-data files. */
+int meso_initial(meso_ctx *ctx);
+
+/*
+ * nsteps x do_step() (cdugks_shakhov.cpp:724-764, cdugks.cpp:337-371,
+ * dugks.cpp:346-383), including the residual check every residual_interval
+ * steps and the convergence counter.  Returns early with MESO_OK when
+ * run_state turns 0 by convergence, and with MESO_ERR_NAN when it turns 0 by
+ * an unmasked NaN / T < 0 cell.  steps_done (may be NULL) receives the count.
+ */
+int meso_step(meso_ctx *ctx, int32_t nsteps, int32_t *steps_done);
+
+/* Macroscopic cell fields rho_cell, vel_cell, T_cell, q_cell (any pointer may be NULL). */
+int meso_get_macros(meso_ctx *ctx, double *rho, double *u, double *T, double *q);
+
+/* Shakhov flux moments of the last step (flux_m0, flux_m1, flux_m2; cdugks_shakhov.cpp:636-641). */
+int meso_get_flux_moments(meso_ctx *ctx, double *m0, double *m1, double *m2);
+
+int meso_get_status(meso_ctx *ctx, meso_status *st);
+
+/* update_config() (cdugks_shakhov.cpp:7-33): new settings take effect from the next step.
+ * solver, precision and K may not change. */
+int meso_set_params(meso_ctx *ctx, const meso_params *params);
+int meso_get_params(meso_ctx *ctx, meso_params *params);
+
+/* output() of the reference (Tecplot data.plt / grid.plt and the np text files), for case contexts. */
+int meso_output(meso_ctx *ctx);
+
+/* Exact device-state snapshot (distribution functions + macros + step counters). */
+size_t meso_snapshot_size(meso_ctx *ctx);
+int meso_snapshot(meso_ctx *ctx, void *host, size_t bytes);
+int meso_restore(meso_ctx *ctx, const void *host, size_t bytes);
+
+/* Device bytes this context holds. */
+size_t meso_ctx_device_bytes(meso_ctx *ctx);
+
+/* Time of the last meso_step call on the device, in ms (CUDA events around the launches). */
+double meso_last_step_ms(meso_ctx *ctx);
+
+/* Number of kernel launches the last meso_step call issued. */
+int64_t meso_last_step_launches(meso_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MESO_GPU_H */

@@ -1,0 +1,921 @@
+// C ABI of the step library (include/meso_gpu.h): context lifecycle, upload,
+// the do_step loop with the reference's residual / convergence logic, and the
+// read-back of macroscopic fields in the original cell order.
+//
+// Reference correspondence (meso-lts):
+//   step loop              src/meso/exec.cpp:141-165
+//   do_step bookkeeping    cdugks_shakhov.cpp:724-764, cdugks.cpp:337-371, dugks.cpp:346-383
+//   residual               src/solver/field.cpp:223-249, src/core/core.cpp:45-51
+//   derived constants      cdugks.cpp:41-47, 171, 306-308; dugks.cpp:41-48, 300, 331;
+//                          cdugks_shakhov.cpp:29-32
+#include "capi_internal.h"
+
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+#include "host/output.h"
+
+namespace meso_host {
+
+namespace {
+thread_local std::string g_error;
+}
+
+const char *last_error_cstr() { return g_error.c_str(); }
+
+void set_error(const std::string &msg) { g_error = msg; }
+int fail(int code, const std::string &msg) {
+    g_error = msg;
+    return code;
+}
+
+template <class T> T *DevArena::alloc(size_t n) {
+    if (n == 0) n = 1;
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) throw std::bad_alloc();
+    ptrs.push_back(p);
+    bytes += n * sizeof(T);
+    return static_cast<T *>(p);
+}
+
+void DevArena::release() {
+    for (void *p : ptrs) cudaFree(p);
+    ptrs.clear();
+    bytes = 0;
+}
+
+void derive_kparams(const meso_params &p, int dim, meso::KParams &k) {
+    std::memset(&k, 0, sizeof(k));
+    k.dt = p.dt;
+    k.hdt = p.dt * 0.5;
+    k.R = p.R;
+    k.T0 = p.T0;
+    k.Kd = (double)p.K;
+    k.Dd = (double)dim;
+    k.Pr = p.Pr;
+    k.mu0 = p.mu0;
+    k.vhs = p.vhs_index;
+    k.gamma = (p.K + 5.0) / (p.K + 3.0);
+    k.Cv = (p.K + 3.0) * p.R * 0.5;
+    k.venkata_k = p.venkata_k;
+    k.gradient = p.gradient_switch;
+    k.limiter = p.limiter_switch;
+    if (p.solver != MESO_SOLVER_CDUGKS_SHAKHOV) {
+        k.RT = p.R * p.T0;
+        k.over_RT = 1.0 / k.RT;
+        double c_sound = std::sqrt(k.RT);
+        k.tau = (p.L0 * p.Ma) / (p.Re * c_sound);
+        k.hdt = 0.5 * p.dt;
+        k.cm = k.hdt / (k.hdt - 2.0 * k.tau);
+        k.Cc = k.tau / (k.tau + k.hdt);
+        k.c_eq = k.hdt / (2.0 * k.tau);
+        k.c_eq_face = k.hdt / (2.0 * k.tau + k.hdt);
+        k.C_bp_to_t = (p.dt + k.hdt) / (k.hdt - 2.0 * k.tau);
+        k.C_t_to_bp = (p.dt + k.hdt) / (2.0 * k.tau + p.dt);
+    }
+}
+
+}  // namespace meso_host
+
+using namespace meso_host;
+
+namespace {
+
+#define CUDA_TRY(expr)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (expr);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return fail(MESO_ERR_CUDA, std::string(#expr ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+bool valid_params(const meso_params &p, std::string &why) {
+    if (p.solver < 0 || p.solver > 2) { why = "unknown solver kind"; return false; }
+    if (p.precision != MESO_FP64 && p.precision != MESO_FP32) { why = "unknown precision"; return false; }
+    if (!(p.dt > 0.0) || !std::isfinite(p.dt)) { why = "timeStep must be positive"; return false; }
+    if (p.residual_interval < 0) { why = "residual_interval must be >= 0"; return false; }
+    return true;
+}
+
+template <class T> void upload(T *dst, const std::vector<T> &src, cudaStream_t s) {
+    if (!src.empty()) cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+int check_desc(const meso_mesh_desc *m, const meso_dvs_desc *d, const meso_mark_desc *marks, int nmarks) {
+    if (!m || !d) return fail(MESO_ERR_INVALID, "null mesh or DVS descriptor");
+    if (m->dim != 2 && m->dim != 3) return fail(MESO_ERR_INVALID, "mesh dim must be 2 or 3");
+    if (m->ncell <= 0 || m->nface <= 0) return fail(MESO_ERR_INVALID, "empty mesh");
+    if (d->nv <= 0 || !d->xi || !d->w) return fail(MESO_ERR_INVALID, "empty DVS");
+    if (!m->cell_pos || !m->cell_vol || !m->cell_face_ptr || !m->cell_face || !m->cell_nbr_ptr ||
+        !m->lsq_c || !m->face_cell || !m->face_pos || !m->face_area || !m->face_normal || !m->face_mark)
+        return fail(MESO_ERR_INVALID, "mesh descriptor has a null table");
+    if (nmarks <= 0 || !marks) return fail(MESO_ERR_INVALID, "mark table is empty");
+    for (int c = 0; c < m->ncell; ++c) {
+        if (m->cell_face_ptr[c + 1] < m->cell_face_ptr[c] || m->cell_nbr_ptr[c + 1] < m->cell_nbr_ptr[c])
+            return fail(MESO_ERR_INVALID, "CSR pointers must be non-decreasing");
+        if (!(m->cell_vol[c] > 0.0)) return fail(MESO_ERR_INVALID, "cell volume must be positive");
+    }
+    const int nf = m->cell_face_ptr[m->ncell], nn = m->cell_nbr_ptr[m->ncell];
+    for (int j = 0; j < nf; ++j)
+        if (m->cell_face[j] < 0 || m->cell_face[j] >= m->nface) return fail(MESO_ERR_INVALID, "cell_face out of range");
+    for (int j = 0; j < nn; ++j)
+        if (m->cell_nbr[j] < 0 || m->cell_nbr[j] >= m->ncell) return fail(MESO_ERR_INVALID, "cell_nbr out of range");
+    if (nn > 0 && (!m->lsq_w || !m->lsq_dr)) return fail(MESO_ERR_INVALID, "least-squares tables missing");
+    for (int f = 0; f < m->nface; ++f) {
+        for (int s = 0; s < 2; ++s)
+            if (m->face_cell[2 * f + s] < 0 || m->face_cell[2 * f + s] >= m->ncell)
+                return fail(MESO_ERR_INVALID, "face_cell out of range");
+        if (m->face_mark[f] < 0 || m->face_mark[f] >= nmarks) return fail(MESO_ERR_INVALID, "face_mark out of range");
+    }
+    for (int i = 0; i < nmarks; ++i)
+        if (marks[i].type < 0 || marks[i].type > MESO_BC_SYMMETRY) return fail(MESO_ERR_INVALID, "bad mark type");
+    if (d->sym)
+        for (int p = 0; p < 3 * d->nv; ++p)
+            if (d->sym[p] < 0 || d->sym[p] >= d->nv) return fail(MESO_ERR_INVALID, "DVS symmetry index out of range");
+    for (int i = 0; i < nmarks; ++i)
+        if ((marks[i].type == MESO_BC_SYMMETRY || marks[i].type == MESO_BC_SLIP_WALL) &&
+            (marks[i].direction < 0 || marks[i].direction > 2))
+            return fail(MESO_ERR_INVALID, "symmetry direction must be 0, 1 or 2");
+    return MESO_OK;
+}
+
+// Host macro arrays in renumbered order <-> original order.
+void to_orig(const meso_ctx *c, const std::vector<double> &dev, double *out, int ncomp) {
+    for (int i = 0; i < c->C; ++i) {
+        int o = c->rn.cell_new2old[i];
+        for (int k = 0; k < ncomp; ++k) out[(size_t)o * ncomp + k] = dev[(size_t)i * ncomp + k];
+    }
+}
+void to_new(const meso_ctx *c, const double *in, std::vector<double> &dev, int ncomp) {
+    dev.resize((size_t)c->C * ncomp);
+    for (int i = 0; i < c->C; ++i) {
+        int o = c->rn.cell_new2old[i];
+        for (int k = 0; k < ncomp; ++k) dev[(size_t)i * ncomp + k] = in[(size_t)o * ncomp + k];
+    }
+}
+
+int build_device(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d) {
+    CUDA_TRY(cudaGetDevice(&c->device));
+    CUDA_TRY(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
+    CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&c->ev0));
+    CUDA_TRY(cudaEventCreate(&c->ev1));
+    CUDA_TRY(cudaMallocHost(&c->h_status, sizeof(meso::DStatus)));
+    const int C = m->ncell, F = m->nface, NV = d->nv, D = m->dim;
+    const auto &rn = c->rn;
+    // ---- renumbered host tables
+    std::vector<double> vol(C), cpos(3 * C), lsq_c(9 * C), lsq_w, lsq_dr, farea(F), fpos(3 * F), fn(3 * F);
+    std::vector<int> cf_ptr(1, 0), cf_face, cn_ptr(1, 0), cn_cell, fown(F), fnei(F), fmark(F), bface;
+    std::vector<uint8_t> mask(C, 0);
+    for (int i = 0; i < C; ++i) {
+        int o = rn.cell_new2old[i];
+        vol[i] = m->cell_vol[o];
+        for (int k = 0; k < 3; ++k) cpos[3 * i + k] = m->cell_pos[3 * o + k];
+        for (int k = 0; k < 9; ++k) lsq_c[9 * i + k] = m->lsq_c[9 * o + k];
+        for (int j = m->cell_face_ptr[o]; j < m->cell_face_ptr[o + 1]; ++j) cf_face.push_back(rn.face_old2new[m->cell_face[j]]);
+        cf_ptr.push_back((int)cf_face.size());
+        for (int j = m->cell_nbr_ptr[o]; j < m->cell_nbr_ptr[o + 1]; ++j) {
+            cn_cell.push_back(rn.cell_old2new[m->cell_nbr[j]]);
+            lsq_w.push_back(m->lsq_w[j]);
+            for (int k = 0; k < 3; ++k) lsq_dr.push_back(m->lsq_dr[3 * j + k]);
+        }
+        cn_ptr.push_back((int)cn_cell.size());
+        if (!c->mask.empty()) mask[i] = c->mask[o];
+    }
+    for (int f = 0; f < F; ++f) {
+        int o = rn.face_new2old[f];
+        fown[f] = rn.cell_old2new[m->face_cell[2 * o]];
+        fnei[f] = rn.cell_old2new[m->face_cell[2 * o + 1]];
+        farea[f] = m->face_area[o];
+        for (int k = 0; k < 3; ++k) {
+            fpos[3 * f + k] = m->face_pos[3 * o + k];
+            fn[3 * f + k] = m->face_normal[3 * o + k];
+        }
+        fmark[f] = m->face_mark[o];
+        if (c->marks[fmark[f]].type != MESO_BC_FLUID_INTERIOR) bface.push_back(f);
+    }
+    std::vector<double> xix(NV), xiy(NV), xiz(NV), w(NV);
+    std::vector<int> sym(3 * NV, 0);
+    for (int p = 0; p < NV; ++p) {
+        xix[p] = d->xi[3 * p];
+        xiy[p] = d->xi[3 * p + 1];
+        xiz[p] = d->xi[3 * p + 2];
+        w[p] = d->w[p];
+        if (d->sym)
+            for (int k = 0; k < 3; ++k) sym[3 * p + k] = d->sym[3 * p + k];
+    }
+    c->nb = (int)bface.size();
+    auto &A = c->arena;
+    auto &dm = c->dm;
+    dm.dim = D;
+    dm.C = C;
+    dm.F = F;
+    dm.NV = NV;
+    dm.nb = c->nb;
+    try {
+        double *p_vol = A.alloc<double>(C), *p_cpos = A.alloc<double>(3 * C), *p_lsqc = A.alloc<double>(9 * C);
+        double *p_lw = A.alloc<double>(lsq_w.size()), *p_ldr = A.alloc<double>(lsq_dr.size());
+        int *p_cfp = A.alloc<int>(C + 1), *p_cf = A.alloc<int>(cf_face.size()), *p_cnp = A.alloc<int>(C + 1);
+        int *p_cn = A.alloc<int>(cn_cell.size());
+        int *p_fo = A.alloc<int>(F), *p_fne = A.alloc<int>(F), *p_fm = A.alloc<int>(F), *p_bf = A.alloc<int>(bface.size());
+        double *p_fa = A.alloc<double>(F), *p_fp = A.alloc<double>(3 * F), *p_fn = A.alloc<double>(3 * F);
+        double *p_x = A.alloc<double>(NV), *p_y = A.alloc<double>(NV), *p_z = A.alloc<double>(NV), *p_w = A.alloc<double>(NV);
+        int *p_sym = A.alloc<int>(3 * NV);
+        meso_mark_desc *p_marks = A.alloc<meso_mark_desc>(c->marks.size());
+        uint8_t *p_mask = A.alloc<uint8_t>(C);
+        upload(p_vol, vol, c->stream);
+        upload(p_cpos, cpos, c->stream);
+        upload(p_lsqc, lsq_c, c->stream);
+        upload(p_lw, lsq_w, c->stream);
+        upload(p_ldr, lsq_dr, c->stream);
+        upload(p_cfp, cf_ptr, c->stream);
+        upload(p_cf, cf_face, c->stream);
+        upload(p_cnp, cn_ptr, c->stream);
+        upload(p_cn, cn_cell, c->stream);
+        upload(p_fo, fown, c->stream);
+        upload(p_fne, fnei, c->stream);
+        upload(p_fm, fmark, c->stream);
+        upload(p_bf, bface, c->stream);
+        upload(p_fa, farea, c->stream);
+        upload(p_fp, fpos, c->stream);
+        upload(p_fn, fn, c->stream);
+        upload(p_x, xix, c->stream);
+        upload(p_y, xiy, c->stream);
+        upload(p_z, xiz, c->stream);
+        upload(p_w, w, c->stream);
+        upload(p_sym, sym, c->stream);
+        upload(p_marks, c->marks, c->stream);
+        upload(p_mask, mask, c->stream);
+        dm.vol = p_vol;
+        dm.cpos = p_cpos;
+        dm.cf_ptr = p_cfp;
+        dm.cf_face = p_cf;
+        dm.cn_ptr = p_cnp;
+        dm.cn_cell = p_cn;
+        dm.lsq_w = p_lw;
+        dm.lsq_dr = p_ldr;
+        dm.lsq_c = p_lsqc;
+        dm.fown = p_fo;
+        dm.fnei = p_fne;
+        dm.farea = p_fa;
+        dm.fpos = p_fp;
+        dm.fn = p_fn;
+        dm.fmark = p_fm;
+        dm.bface = p_bf;
+        dm.xix = p_x;
+        dm.xiy = p_y;
+        dm.xiz = p_z;
+        dm.w = p_w;
+        dm.sym = p_sym;
+        dm.marks = p_marks;
+        dm.mask = p_mask;
+        c->d_status = A.alloc<meso::DStatus>(1);
+
+        const bool shakhov = c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV;
+        const size_t cv = (size_t)C * NV, fv = (size_t)F * NV, bv = (size_t)std::max(c->nb, 1) * NV;
+        if (c->params.precision == MESO_FP32)
+            return fail(MESO_ERR_UNSUPPORTED, "FP32 storage is not available in this build");
+        auto &s = c->ps;
+        s.solver = c->params.solver;
+        s.num_sms = c->num_sms;
+        s.mesh = dm;
+        s.status = c->d_status;
+        s.f0 = A.alloc<double>(cv);
+        s.f1 = shakhov ? A.alloc<double>(cv) : nullptr;
+        s.face0 = A.alloc<double>(fv);
+        s.face1 = shakhov ? A.alloc<double>(fv) : nullptr;
+        s.grad0 = A.alloc<double>(cv * D);
+        s.grad1 = shakhov ? A.alloc<double>(cv * D) : nullptr;
+        s.flux0 = c->params.solver != MESO_SOLVER_DUGKS ? A.alloc<double>(cv) : nullptr;
+        s.flux1 = shakhov ? A.alloc<double>(cv) : nullptr;
+        s.snap0 = A.alloc<double>(bv);
+        s.snap1 = shakhov ? A.alloc<double>(bv) : nullptr;
+        s.rho = A.alloc<double>(C);
+        s.u = A.alloc<double>(3 * C);
+        s.T = A.alloc<double>(C);
+        s.q = A.alloc<double>(3 * C);
+        s.fm0 = A.alloc<double>(C);
+        s.fm1 = A.alloc<double>(3 * C);
+        s.fm2 = A.alloc<double>(C);
+        s.repair_list = A.alloc<int>(C);
+        CUDA_TRY(cudaMemsetAsync(s.T, 0, sizeof(double) * C, c->stream));
+        CUDA_TRY(cudaMemsetAsync(s.q, 0, sizeof(double) * 3 * C, c->stream));
+        CUDA_TRY(cudaMemsetAsync(s.fm0, 0, sizeof(double) * C, c->stream));
+        CUDA_TRY(cudaMemsetAsync(s.fm1, 0, sizeof(double) * 3 * C, c->stream));
+        CUDA_TRY(cudaMemsetAsync(s.fm2, 0, sizeof(double) * C, c->stream));
+    } catch (const std::bad_alloc &) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        cudaGetLastError();
+        return fail(MESO_ERR_OOM, "device allocation failed (" + std::to_string(A.bytes) + " bytes held, " +
+                                      std::to_string(fr) + " free)");
+    }
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return MESO_OK;
+}
+
+void reset_status(meso_ctx *c) {
+    meso::DStatus s{};
+    s.step = 0;
+    s.stop_step = INT_MAX;
+    s.first_bad = INT_MAX;
+    std::memcpy(c->h_status, &s, sizeof(s));
+    cudaMemcpyAsync(c->d_status, c->h_status, sizeof(s), cudaMemcpyHostToDevice, c->stream);
+    cudaStreamSynchronize(c->stream);
+}
+
+int read_status(meso_ctx *c) {
+    CUDA_TRY(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(meso::DStatus), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return MESO_OK;
+}
+
+int download_macros(meso_ctx *c, std::vector<double> &rho, std::vector<double> &u, std::vector<double> &T,
+                    std::vector<double> &q) {
+    const int C = c->C;
+    std::vector<double> r(C), uu(3 * C), t(C), qq(3 * C);
+    CUDA_TRY(cudaMemcpyAsync(r.data(), c->ps.rho, sizeof(double) * C, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(uu.data(), c->ps.u, sizeof(double) * 3 * C, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(t.data(), c->ps.T, sizeof(double) * C, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(qq.data(), c->ps.q, sizeof(double) * 3 * C, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    rho.resize(C);
+    u.resize(3 * C);
+    T.resize(C);
+    q.resize(3 * C);
+    to_orig(c, r, rho.data(), 1);
+    to_orig(c, uu, u.data(), 3);
+    to_orig(c, t, T.data(), 1);
+    to_orig(c, qq, q.data(), 3);
+    return MESO_OK;
+}
+
+// Solver::residual (field.cpp:223-249): sum |(new-old)/old| V/V_total in cell order; old <- new.
+double residual_scalar(const meso_ctx *c, std::vector<double> &old, const std::vector<double> &nw) {
+    double r = 0.0;
+    for (int i = 0; i < c->C; ++i) r += std::abs((nw[i] - old[i]) / old[i]) * (c->vol[i] / c->total_volume);
+    old = nw;
+    return r;
+}
+void residual_vector(const meso_ctx *c, std::vector<double> &old, const std::vector<double> &nw, double out[3]) {
+    double rx = 0, ry = 0, rz = 0;
+    for (int i = 0; i < c->C; ++i) {
+        double vx = std::fabs((nw[3 * i] - old[3 * i]) / old[3 * i]);
+        double vy = std::fabs((nw[3 * i + 1] - old[3 * i + 1]) / old[3 * i + 1]);
+        double vz = std::fabs((nw[3 * i + 2] - old[3 * i + 2]) / old[3 * i + 2]);
+        double s = c->vol[i] / c->total_volume;
+        rx += vx * s;
+        ry += vy * s;
+        rz += vz * s;
+    }
+    old = nw;
+    out[0] = rx;
+    out[1] = ry;
+    out[2] = rz;
+}
+
+// Residual check of do_step (e.g. cdugks_shakhov.cpp:729-757).
+int residual_check(meso_ctx *c) {
+    std::vector<double> rho, u, T, q;
+    int rc = download_macros(c, rho, u, T, q);
+    if (rc) return rc;
+    double rr = residual_scalar(c, c->rho_res, rho);
+    double ru[3];
+    residual_vector(c, c->u_res, u, ru);
+    std::vector<double> list;
+    if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV) {
+        double rT = residual_scalar(c, c->T_res, T);
+        double rq[3];
+        residual_vector(c, c->q_res, q, rq);
+        if (c->dim == 2) list = {rr, rT, ru[0], ru[1], rq[0], rq[1]};
+        else list = {rr, rT, ru[0], ru[1], ru[2], rq[0], rq[1], rq[2]};
+    } else {
+        if (c->dim == 2) list = {rr, ru[0], ru[1]};
+        else list = {rr, ru[0], ru[1], ru[2]};
+    }
+    c->nres = (int)list.size();
+    for (int i = 0; i < c->nres; ++i) c->last_res[i] = list[i];
+    bool conv = true;
+    for (double v : list) conv = conv && (v <= c->params.residual_limit);
+    if (conv) c->converge_state++;
+    else c->converge_state = 0;
+    if (c->converge_state >= 10) {
+        c->run_state = 0;
+        c->converged = 1;
+    }
+    return MESO_OK;
+}
+
+int launch_step(meso_ctx *c) {
+    int rc = meso::plain_step(c->ps, c->stream, &c->last_launches);
+    if (rc) return fail(MESO_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+    return MESO_OK;
+}
+
+// Live reload of [settings] (cdugks_shakhov.cpp:762): the reference re-reads
+// the case file after every step; re-reading only when its mtime changed
+// gives the same settings without a file read per step.
+void maybe_reload(meso_ctx *c) {
+    if (!c->kase || c->params.solver != MESO_SOLVER_CDUGKS_SHAKHOV) return;
+    struct stat sb;
+    if (stat(c->kase->config.path().c_str(), &sb) != 0) return;
+    if (sb.st_mtime == c->case_mtime) return;
+    c->case_mtime = sb.st_mtime;
+    try {
+        c->kase->params.precision = c->params.precision;
+        if (c->kase->reload_settings()) {
+            c->params = c->kase->params;
+            derive_kparams(c->params, c->dim, c->ps.kp);
+        }
+    } catch (...) {
+        // a half-written file keeps the current settings; the next change retries
+    }
+}
+
+meso_ctx *new_ctx(const meso_mesh_desc *m, const meso_dvs_desc *d, const meso_mark_desc *marks, int nmarks,
+                  const meso_params *p, const uint8_t *mask, int *rc) {
+    auto c = std::make_unique<meso_ctx>();
+    c->params = *p;
+    c->dim = m->dim;
+    c->C = m->ncell;
+    c->F = m->nface;
+    c->NV = d->nv;
+    c->marks.assign(marks, marks + nmarks);
+    if (mask) c->mask.assign(mask, mask + m->ncell);
+    c->vol.assign(m->cell_vol, m->cell_vol + m->ncell);
+    c->min_cell_size = m->min_cell_size;
+    c->total_volume = m->total_volume;
+    if (!(c->total_volume > 0.0)) {
+        c->total_volume = 0.0;
+        for (double v : c->vol) c->total_volume += v;
+    }
+    c->dvs_max_mag = d->max_magnitude;
+    if (c->params.solver == MESO_SOLVER_DUGKS) {
+        double mm = d->max_magnitude;
+        if (!(mm > 0.0)) {
+            for (int i = 0; i < d->nv; ++i) {
+                double v = std::sqrt(d->xi[3 * i] * d->xi[3 * i] + d->xi[3 * i + 1] * d->xi[3 * i + 1] +
+                                     d->xi[3 * i + 2] * d->xi[3 * i + 2]);
+                mm = std::max(mm, v);
+            }
+        }
+        c->params.dt = c->params.CFL * (c->min_cell_size / mm);  // dugks.cpp:47
+    }
+    std::string why;
+    if (!valid_params(c->params, why)) {
+        *rc = fail(MESO_ERR_INVALID, why);
+        return nullptr;
+    }
+    c->rn = renumber(*m, false);
+    derive_kparams(c->params, c->dim, c->ps.kp);
+    *rc = build_device(c.get(), m, d);
+    if (*rc != MESO_OK) return nullptr;
+    derive_kparams(c->params, c->dim, c->ps.kp);
+    reset_status(c.get());
+    return c.release();
+}
+
+int init_common(meso_ctx *c, const double *rho, const double *u, const double *T, const double *q, int mode) {
+    const int C = c->C;
+    if (!rho || !u) return fail(MESO_ERR_INVALID, "rho and u are required");
+    const bool shakhov = c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV;
+    if (shakhov && !T) return fail(MESO_ERR_INVALID, "T is required for the Shakhov solver");
+    if (mode != 0 && mode != 1) return fail(MESO_ERR_INVALID, "mode must be 0 or 1");
+    std::vector<double> r, uu, t(C, 0.0), qq(3 * (size_t)C, 0.0);
+    to_new(c, rho, r, 1);
+    to_new(c, u, uu, 3);
+    if (T) to_new(c, T, t, 1);
+    if (q && shakhov) to_new(c, q, qq, 3);
+    CUDA_TRY(cudaMemcpyAsync(c->ps.rho, r.data(), sizeof(double) * C, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->ps.u, uu.data(), sizeof(double) * 3 * C, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->ps.T, t.data(), sizeof(double) * C, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->ps.q, qq.data(), sizeof(double) * 3 * C, cudaMemcpyHostToDevice, c->stream));
+    if (meso::plain_init(c->ps, mode, c->stream)) return fail(MESO_ERR_CUDA, "init kernel launch failed");
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    reset_status(c);
+    c->step = 0;
+    c->solution_time = 0.0;
+    c->run_state = 1;
+    c->converged = 0;
+    c->converge_state = 0;
+    c->initialized = true;
+    std::vector<double> T2, q2;
+    int rc = download_macros(c, c->rho_res, c->u_res, T2, q2);
+    if (rc) return rc;
+    c->T_res = T2;
+    c->q_res = q2;
+    return MESO_OK;
+}
+
+std::vector<double> read_scalar_file(const std::string &f, int n) {
+    MESO::Field<double> fld;
+    fld.len = n;
+    fld.values.assign(n, 0.0);
+    MESO::read_np_data<double>(f, fld);
+    return fld.values;
+}
+std::vector<double> read_vector_file(const std::string &f, int n) {
+    MESO::Field<MESO::Vector> fld;
+    fld.len = n;
+    fld.values.assign(n, MESO::Vector());
+    MESO::read_np_data<MESO::Vector>(f, fld);
+    std::vector<double> out(3 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        out[3 * i] = fld.values[i].x;
+        out[3 * i + 1] = fld.values[i].y;
+        out[3 * i + 2] = fld.values[i].z;
+    }
+    return out;
+}
+
+#define CTX_CHECK(c)                                                        \
+    do {                                                                    \
+        if (!(c)) return fail(MESO_ERR_INVALID, "null context");            \
+        if (cudaSetDevice((c)->device) != cudaSuccess)                      \
+            return fail(MESO_ERR_CUDA, "cannot select the context's device"); \
+    } while (0)
+
+}  // namespace
+
+extern "C" {
+
+const char *meso_last_error(void) { return last_error_cstr(); }
+
+const char *meso_version(void) { return "meso-gb300 1.0 sm_103a (FP64 plain step)"; }
+
+int meso_case_load(const char *case_file, meso_case **out) {
+    if (!case_file || !out) return fail(MESO_ERR_INVALID, "null argument");
+    *out = nullptr;
+    try {
+        *out = load_case(case_file).release();
+        return MESO_OK;
+    } catch (const std::invalid_argument &e) {
+        std::string msg = e.what();
+        bool io = msg.find("file open error") != std::string::npos;
+        return fail(io ? MESO_ERR_IO : MESO_ERR_INVALID, msg);
+    } catch (const std::exception &e) {
+        return fail(MESO_ERR_IO, std::string("case load failed: ") + e.what());
+    }
+}
+
+void meso_case_free(meso_case *c) { delete c; }
+
+int meso_case_mesh(const meso_case *c, meso_mesh_desc *m) {
+    if (!c || !m) return fail(MESO_ERR_INVALID, "null argument");
+    c->mesh_desc(*m);
+    return MESO_OK;
+}
+
+int meso_case_dvs(const meso_case *c, meso_dvs_desc *d) {
+    if (!c || !d) return fail(MESO_ERR_INVALID, "null argument");
+    c->dvs_desc(*d);
+    return MESO_OK;
+}
+
+int meso_case_marks(const meso_case *c, const meso_mark_desc **marks, int32_t *n) {
+    if (!c || !marks || !n) return fail(MESO_ERR_INVALID, "null argument");
+    *marks = c->marks.data();
+    *n = (int32_t)c->marks.size();
+    return MESO_OK;
+}
+
+int meso_case_params(const meso_case *c, meso_params *p) {
+    if (!c || !p) return fail(MESO_ERR_INVALID, "null argument");
+    *p = c->params;
+    return MESO_OK;
+}
+
+int meso_case_initial_fields(const meso_case *c, double *rho, double *u, double *T, uint8_t *mask) {
+    if (!c) return fail(MESO_ERR_INVALID, "null argument");
+    try {
+        c->initial_fields(rho, u, T, mask);
+    } catch (const std::exception &e) {
+        return fail(MESO_ERR_INVALID, e.what());
+    }
+    return MESO_OK;
+}
+
+int meso_case_loop_settings(const meso_case *c, int32_t *max_step, int32_t *write_interval, int32_t *read_np_data,
+                            int32_t *output_latest, int32_t *output_np) {
+    if (!c) return fail(MESO_ERR_INVALID, "null argument");
+    if (max_step) *max_step = c->max_step;
+    if (write_interval) *write_interval = c->write_interval;
+    if (read_np_data) *read_np_data = c->read_np_data;
+    if (output_latest) *output_latest = c->output_latest;
+    if (output_np) *output_np = c->output_np;
+    return MESO_OK;
+}
+
+int meso_ctx_create(const meso_mesh_desc *mesh, const meso_dvs_desc *dvs, const meso_mark_desc *marks, int32_t nmarks,
+                    const meso_params *params, const uint8_t *mask, meso_ctx **out) {
+    if (!out || !params) return fail(MESO_ERR_INVALID, "null argument");
+    *out = nullptr;
+    int rc = check_desc(mesh, dvs, marks, nmarks);
+    if (rc) return rc;
+    try {
+        meso_ctx *c = new_ctx(mesh, dvs, marks, nmarks, params, mask, &rc);
+        if (!c) return rc;
+        *out = c;
+        return MESO_OK;
+    } catch (const std::exception &e) {
+        return fail(MESO_ERR_INVALID, e.what());
+    }
+}
+
+int meso_ctx_create_from_case(const char *case_file, int32_t precision, meso_ctx **out) {
+    if (!out) return fail(MESO_ERR_INVALID, "null argument");
+    *out = nullptr;
+    meso_case *k = nullptr;
+    int rc = meso_case_load(case_file, &k);
+    if (rc) return rc;
+    std::unique_ptr<meso_case> kase(k);
+    if (precision == MESO_FP64 || precision == MESO_FP32) kase->params.precision = precision;
+    meso_mesh_desc m;
+    meso_dvs_desc d;
+    kase->mesh_desc(m);
+    kase->dvs_desc(d);
+    std::vector<uint8_t> mask(kase->mesh.NCELL, 0);
+    try {
+        kase->initial_fields(nullptr, nullptr, nullptr, mask.data());
+    } catch (const std::exception &e) {
+        return fail(MESO_ERR_INVALID, e.what());
+    }
+    rc = meso_ctx_create(&m, &d, kase->marks.data(), (int)kase->marks.size(), &kase->params, mask.data(), out);
+    if (rc) return rc;
+    struct stat sb;
+    if (stat(kase->config.path().c_str(), &sb) == 0) (*out)->case_mtime = sb.st_mtime;
+    (*out)->kase = std::move(kase);
+    return MESO_OK;
+}
+
+void meso_ctx_destroy(meso_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->arena.release();
+    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int meso_init_macros(meso_ctx *c, const double *rho, const double *u, const double *T, const double *q, int32_t mode) {
+    CTX_CHECK(c);
+    return init_common(c, rho, u, T, q, mode);
+}
+
+int meso_initial(meso_ctx *c) {
+    CTX_CHECK(c);
+    if (!c->kase) return fail(MESO_ERR_INVALID, "meso_initial needs a context made from a case file");
+    const int C = c->C;
+    auto &k = *c->kase;
+    try {
+        if (k.read_np_data) {
+            std::vector<double> rho, u, T, q;
+            if (c->params.solver == MESO_SOLVER_DUGKS) {
+                // dugks.cpp:57-59
+                rho = read_scalar_file(k.case_name + "/np-data/Rho.np.dat", C);
+                u = read_vector_file(k.case_name + "/np-data/vel.np.dat", C);
+            } else {
+                rho = read_scalar_file(k.case_name + "/latest/Rho", C);
+                u = read_vector_file(k.case_name + "/latest/U", C);
+                if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV) {
+                    T = read_scalar_file(k.case_name + "/latest/T", C);
+                    q = read_vector_file(k.case_name + "/latest/q", C);
+                }
+            }
+            return init_common(c, rho.data(), u.data(), T.empty() ? nullptr : T.data(),
+                               q.empty() ? nullptr : q.data(), 1);
+        }
+        std::vector<double> rho(C), u(3 * (size_t)C), T(C);
+        k.initial_fields(rho.data(), u.data(), T.data(), nullptr);
+        return init_common(c, rho.data(), u.data(), T.data(), nullptr, 0);
+    } catch (const std::exception &e) {
+        return fail(MESO_ERR_IO, e.what());
+    }
+}
+
+int meso_step(meso_ctx *c, int32_t nsteps, int32_t *steps_done) {
+    CTX_CHECK(c);
+    if (steps_done) *steps_done = 0;
+    if (!c->initialized) return fail(MESO_ERR_INVALID, "meso_step before initial()");
+    if (nsteps < 0) return fail(MESO_ERR_INVALID, "nsteps must be >= 0");
+    const int start = c->step;
+    std::vector<double> dts;
+    dts.reserve(nsteps);
+    c->last_launches = 0;
+    CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+    int issued = 0;
+    bool stopped = false;
+    for (int i = 0; i < nsteps && c->run_state; ++i) {
+        maybe_reload(c);
+        int rc = launch_step(c);
+        if (rc) return rc;
+        dts.push_back(c->params.dt);
+        ++issued;
+        const int s = start + issued;
+        const int ri = c->params.residual_interval;
+        if (ri > 0 && s % ri == 0) {
+            rc = read_status(c);
+            if (rc) return rc;
+            if (c->h_status->stop_step != INT_MAX) {
+                stopped = true;
+                break;
+            }
+            rc = residual_check(c);
+            if (rc) return rc;
+        }
+    }
+    CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
+    int rc = read_status(c);
+    if (rc) return rc;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->last_ms = ms;
+    const int done = c->h_status->step - start;
+    for (int i = 0; i < done && i < (int)dts.size(); ++i) c->solution_time += dts[i];
+    c->step = c->h_status->step;
+    if (steps_done) *steps_done = done;
+    if (stopped || c->h_status->stop_step != INT_MAX) {
+        c->run_state = 0;
+        return fail(MESO_ERR_NAN, "cell " + std::to_string(c->rn.cell_new2old[std::min(c->h_status->first_bad, c->C - 1)]) +
+                                      " caught rho = NaN or T < 0 (no mask)");
+    }
+    return MESO_OK;
+}
+
+int meso_get_macros(meso_ctx *c, double *rho, double *u, double *T, double *q) {
+    CTX_CHECK(c);
+    std::vector<double> r, uu, t, qq;
+    int rc = download_macros(c, r, uu, t, qq);
+    if (rc) return rc;
+    if (rho) std::copy(r.begin(), r.end(), rho);
+    if (u) std::copy(uu.begin(), uu.end(), u);
+    if (T) std::copy(t.begin(), t.end(), T);
+    if (q) std::copy(qq.begin(), qq.end(), q);
+    return MESO_OK;
+}
+
+int meso_get_flux_moments(meso_ctx *c, double *m0, double *m1, double *m2) {
+    CTX_CHECK(c);
+    const int C = c->C;
+    std::vector<double> a(C), b(3 * (size_t)C), d(C);
+    CUDA_TRY(cudaMemcpyAsync(a.data(), c->ps.fm0, sizeof(double) * C, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(b.data(), c->ps.fm1, sizeof(double) * 3 * C, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(d.data(), c->ps.fm2, sizeof(double) * C, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (m0) to_orig(c, a, m0, 1);
+    if (m1) to_orig(c, b, m1, 3);
+    if (m2) to_orig(c, d, m2, 1);
+    return MESO_OK;
+}
+
+int meso_get_status(meso_ctx *c, meso_status *st) {
+    CTX_CHECK(c);
+    if (!st) return fail(MESO_ERR_INVALID, "null status");
+    int rc = read_status(c);
+    if (rc) return rc;
+    std::memset(st, 0, sizeof(*st));
+    st->step = c->step;
+    st->run_state = c->run_state;
+    st->converged = c->converged;
+    st->bad_cells = c->h_status->bad_count;
+    st->first_bad_cell = c->h_status->first_bad == INT_MAX ? -1 : c->rn.cell_new2old[c->h_status->first_bad];
+    st->masked_repairs = c->h_status->repairs_total;
+    st->solution_time = c->solution_time;
+    st->nresidual = c->nres;
+    for (int i = 0; i < c->nres; ++i) st->residual[i] = c->last_res[i];
+    return MESO_OK;
+}
+
+int meso_set_params(meso_ctx *c, const meso_params *p) {
+    CTX_CHECK(c);
+    if (!p) return fail(MESO_ERR_INVALID, "null params");
+    if (p->solver != c->params.solver || p->precision != c->params.precision)
+        return fail(MESO_ERR_INVALID, "solver and precision are fixed for a context");
+    std::string why;
+    if (!valid_params(*p, why)) return fail(MESO_ERR_INVALID, why);
+    c->params = *p;
+    derive_kparams(c->params, c->dim, c->ps.kp);
+    return MESO_OK;
+}
+
+int meso_get_params(meso_ctx *c, meso_params *p) {
+    if (!c || !p) return fail(MESO_ERR_INVALID, "null argument");
+    *p = c->params;
+    return MESO_OK;
+}
+
+int meso_output(meso_ctx *c) {
+    CTX_CHECK(c);
+    if (!c->kase) return fail(MESO_ERR_INVALID, "meso_output needs a context made from a case file");
+    std::vector<double> rho, u, T, q, m0(c->C), m1(3 * (size_t)c->C), m2(c->C);
+    int rc = download_macros(c, rho, u, T, q);
+    if (rc) return rc;
+    if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV) {
+        rc = meso_get_flux_moments(c, m0.data(), m1.data(), m2.data());
+        if (rc) return rc;
+    }
+    try {
+        write_solver_output(*c->kase, c->step, c->solution_time, rho, u, T, q, m0, m1, m2);
+    } catch (const std::exception &e) {
+        return fail(MESO_ERR_IO, e.what());
+    }
+    return MESO_OK;
+}
+
+size_t meso_snapshot_size(meso_ctx *c) {
+    if (!c) return 0;
+    const size_t cv = (size_t)c->C * c->NV;
+    const size_t nd = c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV ? 2 : 1;
+    return 64 + sizeof(double) * (nd * cv + 8 * (size_t)c->C) + sizeof(meso::DStatus);
+}
+
+struct SnapHeader {
+    uint32_t magic, C, NV, solver;
+    int32_t step, run_state, converged, converge_state;
+    double solution_time;
+    uint8_t pad[24];
+};
+
+int meso_snapshot(meso_ctx *c, void *host, size_t bytes) {
+    CTX_CHECK(c);
+    if (!host || bytes < meso_snapshot_size(c)) return fail(MESO_ERR_INVALID, "snapshot buffer too small");
+    static_assert(sizeof(SnapHeader) == 64, "header size");
+    SnapHeader h{};
+    h.magic = 0x4D534E50u;
+    h.C = c->C;
+    h.NV = c->NV;
+    h.solver = c->params.solver;
+    h.step = c->step;
+    h.run_state = c->run_state;
+    h.converged = c->converged;
+    h.converge_state = c->converge_state;
+    h.solution_time = c->solution_time;
+    char *p = static_cast<char *>(host);
+    std::memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    const size_t cv = (size_t)c->C * c->NV;
+    auto d2h = [&](const double *src, size_t n) {
+        cudaMemcpyAsync(p, src, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+        p += n * sizeof(double);
+    };
+    d2h(c->ps.f0, cv);
+    if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV) d2h(c->ps.f1, cv);
+    d2h(c->ps.rho, c->C);
+    d2h(c->ps.u, 3 * (size_t)c->C);
+    d2h(c->ps.T, c->C);
+    d2h(c->ps.q, 3 * (size_t)c->C);
+    CUDA_TRY(cudaMemcpyAsync(p, c->d_status, sizeof(meso::DStatus), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return MESO_OK;
+}
+
+int meso_restore(meso_ctx *c, const void *host, size_t bytes) {
+    CTX_CHECK(c);
+    if (!host || bytes < meso_snapshot_size(c)) return fail(MESO_ERR_INVALID, "snapshot buffer too small");
+    SnapHeader h;
+    std::memcpy(&h, host, sizeof(h));
+    if (h.magic != 0x4D534E50u || (int)h.C != c->C || (int)h.NV != c->NV || (int)h.solver != c->params.solver)
+        return fail(MESO_ERR_INVALID, "snapshot does not match this context");
+    const char *p = static_cast<const char *>(host) + sizeof(h);
+    const size_t cv = (size_t)c->C * c->NV;
+    auto h2d = [&](double *dst, size_t n) {
+        cudaMemcpyAsync(dst, p, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+        p += n * sizeof(double);
+    };
+    h2d(c->ps.f0, cv);
+    if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV) h2d(c->ps.f1, cv);
+    h2d(c->ps.rho, c->C);
+    h2d(c->ps.u, 3 * (size_t)c->C);
+    h2d(c->ps.T, c->C);
+    h2d(c->ps.q, 3 * (size_t)c->C);
+    CUDA_TRY(cudaMemcpyAsync(c->d_status, p, sizeof(meso::DStatus), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->step = h.step;
+    c->run_state = h.run_state;
+    c->converged = h.converged;
+    c->converge_state = h.converge_state;
+    c->solution_time = h.solution_time;
+    c->initialized = true;
+    std::vector<double> T2, q2;
+    int rc = download_macros(c, c->rho_res, c->u_res, T2, q2);
+    c->T_res = T2;
+    c->q_res = q2;
+    return rc;
+}
+
+size_t meso_ctx_device_bytes(meso_ctx *c) { return c ? c->arena.bytes : 0; }
+
+double meso_last_step_ms(meso_ctx *c) { return c ? c->last_ms : 0.0; }
+
+int64_t meso_last_step_launches(meso_ctx *c) { return c ? c->last_launches : 0; }
+
+}  // extern "C"

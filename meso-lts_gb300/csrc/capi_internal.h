@@ -1,0 +1,70 @@
+// Internal definition of the C-ABI context (include/meso_gpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <ctime>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "host/case.h"
+#include "host/renumber.h"
+#include "kernels/fp32_step.h"
+#include "kernels/plain_fp64.h"
+#include "meso_gpu.h"
+
+namespace meso_host {
+
+// Tracks the device allocations of one context.
+struct DevArena {
+    std::vector<void *> ptrs;
+    size_t bytes = 0;
+    template <class T> T *alloc(size_t n);
+    void release();
+    ~DevArena() { release(); }
+};
+
+void set_error(const std::string &msg);
+const char *last_error_cstr();
+int fail(int code, const std::string &msg);
+
+void derive_kparams(const meso_params &p, int dim, meso::KParams &k);
+
+}  // namespace meso_host
+
+struct meso_ctx {
+    meso_params params{};
+    std::unique_ptr<meso_case> kase;  // set for contexts made from a case file
+    int dim = 2, C = 0, F = 0, NV = 0, nb = 0;
+    meso_host::Renumbering rn;
+    std::vector<meso_mark_desc> marks;
+    std::vector<uint8_t> mask;
+    std::vector<double> vol;  // original order, for residuals
+    double min_cell_size = 0, total_volume = 0, dvs_max_mag = 0;
+
+    // device
+    int device = 0, num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    meso_host::DevArena arena;
+    meso::DMesh dm{};
+    meso::DStatus *d_status = nullptr;
+    meso::DStatus *h_status = nullptr;  // pinned mirror
+    meso::PlainState ps{};
+    meso::Fp32State fs{};
+
+    // host step state (the reference's step / solution_time / run_state / converge_state)
+    int step = 0;
+    double solution_time = 0.0;
+    int run_state = 0;
+    int converged = 0;
+    int converge_state = 0;
+    bool initialized = false;
+    std::vector<double> rho_res, u_res, T_res, q_res;
+    double last_res[8] = {0};
+    int nres = 0;
+    double last_ms = 0.0;
+    int64_t last_launches = 0;
+    std::time_t case_mtime = 0;
+};

@@ -1,0 +1,31 @@
+// Host-visible interface of the plain FP64 step kernels (plain_fp64.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+
+namespace meso {
+
+// Device buffers of one plain-FP64 solve.  f1/face1/... are null for the BGK solvers.
+struct PlainState {
+    int solver;
+    int num_sms;
+    DMesh mesh;
+    KParams kp;
+    DStatus *status;
+    double *f0, *f1;          // [C*NV] cell distributions (g, h for Shakhov)
+    double *face0, *face1;    // [F*NV] face values
+    double *grad0, *grad1;    // [C*NV*dim] gradients
+    double *flux0, *flux1;    // [C*NV] cell fluxes
+    double *snap0, *snap1;    // [nb*NV] boundary snapshots
+    double *rho, *u, *T, *q;  // [C], [3C], [C], [3C]
+    double *fm0, *fm1, *fm2;  // flux moments [C], [3C], [C]
+    int *repair_list;         // [C]
+};
+
+int plain_step(const PlainState &s, cudaStream_t stream, int64_t *launches);
+int plain_init(const PlainState &s, int mode, cudaStream_t stream);
+
+}  // namespace meso
