@@ -83,6 +83,33 @@ def quad_cavity(path: str, n: int, length: float = 1.0) -> dict:
     return dict(ncell=n * n, min_cell_size=2.0 * math.sqrt(h * h / math.pi))
 
 
+def quad_channel(path: str, nx: int, ny: int, lx: float = 2.0, ly: float = 1.0) -> dict:
+    """nx x ny quads on [0,lx]x[0,ly]; marks inlet (x=0), outlet (x=lx), bottom (y=0), top (y=ly)."""
+    hx, hy = lx / nx, ly / ny
+    xs = np.arange(nx + 1) * hx
+    ys = np.arange(ny + 1) * hy
+    xs[-1], ys[-1] = lx, ly
+    X, Y = np.meshgrid(xs, ys)
+    nodes = np.stack([X.ravel(), Y.ravel()], 1)
+    nid = lambda i, j: j * (nx + 1) + i
+    cells = []
+    bc = {"inlet": [], "outlet": [], "bottom": [], "top": []}
+    for j in range(ny):
+        for i in range(nx):
+            c = len(cells)
+            cells.append([nid(i, j), nid(i + 1, j), nid(i + 1, j + 1), nid(i, j + 1)])
+            if j == ny - 1:
+                bc["top"].append((c, 2, 3))
+            if j == 0:
+                bc["bottom"].append((c, 2, 1))
+            if i == nx - 1:
+                bc["outlet"].append((c, 2, 2))
+            if i == 0:
+                bc["inlet"].append((c, 2, 4))
+    _write_neu(path, nodes, cells, 2, bc)
+    return dict(ncell=nx * ny, min_cell_size=2.0 * math.sqrt(hx * hy / math.pi))
+
+
 def _tri_area(p, t):
     a, b, c = p[t[0]], p[t[1]], p[t[2]]
     return 0.5 * ((b[0] - a[0]) * (c[1] - a[1]) - (b[1] - a[1]) * (c[0] - a[0]))
@@ -161,6 +188,99 @@ def tri_cavity(path: str, n: int = 64, seed: int = 0, jitter: float = 0.3) -> di
     _write_neu(path, p, tri, 3, {"lid": lid, "wall": wall})
     amin = min(_tri_area(p, t) for t in tri)
     return dict(ncell=len(tri), min_cell_size=2.0 * math.sqrt(amin / math.pi))
+
+
+def mixed_cavity(path: str, n: int = 64, seed: int = 0, jitter: float = 0.3) -> dict:
+    """Unstructured cavity: a one-cell quad layer along the walls, seeded Delaunay triangles inside.
+
+    Nodes sit on an n x n lattice of spacing h = 1/(n-1); lattice nodes at
+    least two rows from the walls are jittered by up to `jitter` h.  Cells
+    touching a wall are h x h quads (three face neighbours, as in the shipped
+    cavity.neu), the inner square [h, 1-h]^2 is the Delaunay triangulation of
+    its nodes, so every triangle has three neighbours.  (On an all-triangle
+    wall row the reference scheme grows an unstable mode: a boundary triangle
+    has two neighbours and its least-squares gradient is exactly determined.)
+    """
+    from scipy.spatial import Delaunay
+
+    rng = np.random.default_rng(seed)
+    h = 1.0 / (n - 1)
+    idx = {}
+    pts = []
+    for j in range(n):
+        for i in range(n):
+            layer = min(i, j, n - 1 - i, n - 1 - j)
+            x, y = i * h, j * h
+            if i == n - 1:
+                x = 1.0
+            if j == n - 1:
+                y = 1.0
+            if layer >= 2:
+                x += rng.uniform(-jitter, jitter) * h
+                y += rng.uniform(-jitter, jitter) * h
+            idx[(i, j)] = len(pts)
+            pts.append((x, y))
+    p = np.array(pts)
+    cells, types, lid, wall = [], [], [], []
+    for j in range(n - 1):
+        for i in range(n - 1):
+            if not (i == 0 or j == 0 or i == n - 2 or j == n - 2):
+                continue
+            c = len(cells)
+            cells.append([idx[(i, j)], idx[(i + 1, j)], idx[(i + 1, j + 1)], idx[(i, j + 1)]])
+            types.append(2)
+            if j == n - 2:
+                lid.append((c, 2, 3))
+            if j == 0:
+                wall.append((c, 2, 1))
+            if i == n - 2:
+                wall.append((c, 2, 2))
+            if i == 0:
+                wall.append((c, 2, 4))
+    inner = [idx[(i, j)] for j in range(1, n - 1) for i in range(1, n - 1)]
+    tri = Delaunay(p[inner])
+    assert len(np.unique(tri.simplices)) == len(inner), "Delaunay dropped a node"
+    for t in tri.simplices:
+        t = [inner[k] for k in t]
+        if _tri_area(p, t) < 0:
+            t = [t[0], t[2], t[1]]
+        assert _tri_area(p, t) > 1e-14
+        cells.append(t)
+        types.append(3)
+    # conformity: every edge is shared by two cells, except the outer walls
+    em = {}
+    for ci, c in enumerate(cells):
+        for k in range(len(c)):
+            a, b = c[k], c[(k + 1) % len(c)]
+            em.setdefault((min(a, b), max(a, b)), []).append(ci)
+    for (a, b), cs in em.items():
+        on_wall = (p[a, 0] == p[b, 0] and p[a, 0] in (0.0, 1.0)) or (p[a, 1] == p[b, 1] and p[a, 1] in (0.0, 1.0))
+        assert len(cs) == (1 if on_wall else 2), f"non-conforming edge {(a, b)}"
+    _write_neu_mixed(path, p, cells, types, {"lid": lid, "wall": wall})
+    amin = min(abs(_tri_area(p, c)) if len(c) == 3 else h * h for c in cells)
+    return dict(ncell=len(cells), min_cell_size=2.0 * math.sqrt(amin / math.pi))
+
+
+def _write_neu_mixed(path, nodes, cells, types, bcs):
+    """_write_neu for meshes whose cells have different shapes (type per element)."""
+    tmp = path + ".tmp"
+    _write_neu(tmp, nodes, cells, 0, bcs)
+    with open(tmp) as f:
+        lines = f.read().split("\n")
+    out, in_cells, k = [], False, 0
+    for line in lines:
+        if line.strip().startswith("ELEMENTS/CELLS"):
+            in_cells = True
+        elif line.strip() == "ENDOFSECTION":
+            in_cells = False
+        elif in_cells:
+            parts = line.split()
+            line = f"{int(parts[0]):8d} {types[k]:2d} {len(parts) - 3:2d} " + " ".join(f"{int(v):8d}" for v in parts[3:])
+            k += 1
+        out.append(line)
+    with open(path, "w") as f:
+        f.write("\n".join(out))
+    os.remove(tmp)
 
 
 # --------------------------------------------------------------------------- velocity sets
@@ -283,7 +403,12 @@ def shakhov_cavity(d: str, mesh: str = "quad", n: int = 61, dvs: str = "hgh", nv
     """Shakhov CDUGKS cavity (configs 2-4): quad or Delaunay mesh; hGH, NC or D2Q9 velocities."""
     os.makedirs(d, exist_ok=True)
     meshf = os.path.join(d, "mesh.neu")
-    info = quad_cavity(meshf, n) if mesh == "quad" else tri_cavity(meshf, n, seed)
+    if mesh == "quad":
+        info = quad_cavity(meshf, n)
+    elif mesh == "mixed":
+        info = mixed_cavity(meshf, n, seed)
+    else:
+        info = tri_cavity(meshf, n, seed)
     RT = 0.5
     if dvs == "hgh":
         xs = half_range_gh(os.path.join(d, "v.dvs"), nv1d)
@@ -322,8 +447,9 @@ def config1(d: str, steps: int = 2000) -> str:
 
 
 def config2(d: str, steps: int = 500, precision: str = "fp32", n: int = 64, nv1d: int = 101) -> str:
-    """Rarefied Shakhov cavity: ~8k Delaunay triangles, Newton-Cotes 101x101 on [-5,5]^2, Kn 1, lid 0.15."""
-    return shakhov_cavity(d, "tri", n, "nc", nv1d, 1.0, 0.15, steps, seed=0, name="config2", precision=precision)
+    """Rarefied Shakhov cavity: 7686 unstructured cells (7434 Delaunay triangles inside a quad wall layer),
+    Newton-Cotes 101x101 on [-5,5]^2, Kn 1, lid 0.15."""
+    return shakhov_cavity(d, "mixed", n, "nc", nv1d, 1.0, 0.15, steps, seed=0, name="config2", precision=precision)
 
 
 def config3(d: str, steps: int = 5000, precision: str = "fp32") -> str:
@@ -348,3 +474,58 @@ def config4_case(d: str, inst: dict, steps: int = 500, precision: str = "fp32") 
     nv1d = {"d2q9": 3, "hgh": 28, "nc": 101}[inst["dvs"]]
     return shakhov_cavity(d, "quad", inst["side"], inst["dvs"], nv1d, inst["kn"], inst["lid"], steps,
                           name=f"inst{inst['index']}", precision=precision)
+
+
+def shakhov_channel(d: str, kind: str = "pressure", nx: int = 10, ny: int = 6, dvs: str = "hgh", nv1d: int = 8,
+                    kn: float = 0.1, steps: int = 50, name: str = "channel", cfl: float = 0.5,
+                    precision: str = "fp64") -> str:
+    """Shakhov channel exercising the open and mirror boundaries of cdugks_shakhov.cpp:364-607.
+
+    kind = "pressure":  pressure-inlet / pressure-outlet, symmetry bottom, slip-wall top
+    kind = "farfield":  farfield-inlet / farfield-outlet, walls (zeroGradient balance T)
+    kind = "freestream": freestream-inlet / farfield-outlet, symmetry bottom and top
+    """
+    os.makedirs(d, exist_ok=True)
+    info = quad_channel(os.path.join(d, "mesh.neu"), nx, ny)
+    RT = 0.5
+    if dvs == "hgh":
+        xs = half_range_gh(os.path.join(d, "v.dvs"), nv1d)
+        vmax = math.sqrt(2.0) * math.sqrt(2 * RT) * float(np.max(np.abs(xs)))
+        dvs_type = "half-range-Gauss-Hermite"
+    else:
+        newton_cotes(os.path.join(d, "v.dvs"), 1, nv1d - 1, 5.0)
+        vmax = 5.0 * math.sqrt(2.0)
+        dvs_type = "Newton-Cotes"
+    dt = cfl * info["min_cell_size"] / vmax
+    settings = {"solver": "cdugks@shakhov", "case-name": name, "mesh-file": "mesh.neu", "dvs-file": "v.dvs",
+                "dvs-type": dvs_type, "max-step": steps, "Pr": 0.6666666666666667, "gradient-switch": True,
+                "limiter-switch": False, "timeStep": dt, "gas-constant": 0.5, "gas-k": 0, "ref-density": 1.0,
+                "ref-length": 1.0, "ref-temperature": 1.0, "ref-viscosity": viscosity_from_kn(kn),
+                "vhs-index": 0.5, "gpu-precision": precision}
+    if kind == "pressure":
+        marks = [{"name": "inlet", "type": "pressure-inlet", "pressure": _sc(0.52), "temperature": _sc(1.0)},
+                 {"name": "outlet", "type": "pressure-outlet", "pressure": _sc(0.48), "temperature": _sc(1.0)},
+                 {"name": "bottom", "type": "symmetry", "direction": "fixedValue  objectType  1"},
+                 {"name": "top", "type": "slip-wall", "direction": "fixedValue  objectType  1",
+                  "velocity": _vec(0.0), "temperature": _sc(1.0), "slip-wall-alpha-u": _sc(0.7),
+                  "slip-wall-alpha-T": _sc(0.4)}]
+    elif kind == "farfield":
+        marks = [{"name": "inlet", "type": "farfield-inlet", "density": _sc(1.02), "velocity": _vec(0.08),
+                  "temperature": _sc(1.0)},
+                 {"name": "outlet", "type": "farfield-outlet"},
+                 # value line first, then zeroGradient: the balance reads T_cell (cdugks_shakhov.cpp:475-476)
+                 # while the wall set reads the scalar (:533), as in a Patch given both lines
+                 {"name": "bottom", "type": "wall", "velocity": _vec(0.0), "temperature": _sc(1.0),
+                  "temperature ": "zeroGradient"},
+                 {"name": "top", "type": "wall", "velocity": _vec(0.0), "temperature": _sc(1.0)}]
+    elif kind == "freestream":
+        marks = [{"name": "inlet", "type": "freestream-inlet", "pressure": _sc(0.51), "velocity": _vec(0.05),
+                  "temperature": _sc(1.0)},
+                 {"name": "outlet", "type": "farfield-outlet"},
+                 {"name": "bottom", "type": "symmetry", "direction": "fixedValue  objectType  1"},
+                 {"name": "top", "type": "symmetry", "direction": "fixedValue  objectType  1"}]
+    else:
+        raise ValueError(kind)
+    return write_case(os.path.join(d, "case.txt"), settings,
+                      [{"name": "fluid", "density": _sc(1.0), "temperature": _sc(1.0),
+                        "velocity": _vec(0.0)}], marks)
