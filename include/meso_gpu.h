@@ -275,6 +275,16 @@ double meso_last_step_ms(meso_ctx *ctx);
 /* Number of kernel launches the last meso_step call issued. */
 int64_t meso_last_step_launches(meso_ctx *ctx);
 
+/*
+ * Profiling: nsteps real steps (the solution advances) with CUDA events
+ * recorded on the context's stream between the step's kernels; ms[k]
+ * receives the mean device time of phase k per step, *nphases the phase
+ * count.  No counterpart in the reference (which has no timers).
+ */
+int meso_phase_times(meso_ctx *ctx, int32_t nsteps, double *ms, int32_t max_phases, int32_t *nphases);
+/* Kernel name(s) of phase i of this context's step. */
+const char *meso_phase_name(meso_ctx *ctx, int32_t i);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,6 +19,7 @@
 #include <fstream>
 #include <sstream>
 
+#include "host/fp32_host.h"
 #include "host/output.h"
 
 namespace meso_host {
@@ -33,16 +34,6 @@ void set_error(const std::string &msg) { g_error = msg; }
 int fail(int code, const std::string &msg) {
     g_error = msg;
     return code;
-}
-
-template <class T> T *DevArena::alloc(size_t n) {
-    if (n == 0) n = 1;
-    void *p = nullptr;
-    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
-    if (e != cudaSuccess) throw std::bad_alloc();
-    ptrs.push_back(p);
-    bytes += n * sizeof(T);
-    return static_cast<T *>(p);
 }
 
 void DevArena::release() {
@@ -279,8 +270,16 @@ int build_device(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d) {
 
         const bool shakhov = c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV;
         const size_t cv = (size_t)C * NV, fv = (size_t)F * NV, bv = (size_t)std::max(c->nb, 1) * NV;
-        if (c->params.precision == MESO_FP32)
-            return fail(MESO_ERR_UNSUPPORTED, "FP32 storage is not available in this build");
+        if (c->params.precision == MESO_FP32) {
+            c->ps.status = c->d_status;
+            c->ps.mesh = dm;
+            c->ps.solver = c->params.solver;
+            c->ps.num_sms = c->num_sms;
+            if (meso::fp32_configure(c->device)) return fail(MESO_ERR_CUDA, "FP32 kernel configuration failed");
+            int rc = build_fp32_instance(c, m, d, c->plan, 0);
+            if (rc) return rc;
+            return MESO_OK;
+        }
         auto &s = c->ps;
         s.solver = c->params.solver;
         s.num_sms = c->num_sms;
@@ -413,7 +412,8 @@ int residual_check(meso_ctx *c) {
 }
 
 int launch_step(meso_ctx *c) {
-    int rc = meso::plain_step(c->ps, c->stream, &c->last_launches);
+    int rc = c->params.precision == MESO_FP32 ? meso::fp32_step(c->fs, c->stream, &c->last_launches)
+                                              : meso::plain_step(c->ps, c->stream, &c->last_launches);
     if (rc) return fail(MESO_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError()));
     return MESO_OK;
 }
@@ -472,7 +472,19 @@ meso_ctx *new_ctx(const meso_mesh_desc *m, const meso_dvs_desc *d, const meso_ma
         *rc = fail(MESO_ERR_INVALID, why);
         return nullptr;
     }
-    c->rn = renumber(*m, false);
+    if (c->params.precision == MESO_FP32) {
+        if (c->params.solver != MESO_SOLVER_CDUGKS_SHAKHOV || m->dim != 2 || c->params.limiter_switch) {
+            *rc = fail(MESO_ERR_UNSUPPORTED,
+                       "FP32 storage covers the 2-D Shakhov solver without the limiter; use MESO_FP64");
+            return nullptr;
+        }
+        if (!plan_fp32(*m, 64, c->rn, c->plan)) {
+            *rc = fail(MESO_ERR_UNSUPPORTED, "mesh connectivity exceeds the FP32 tile limits");
+            return nullptr;
+        }
+    } else {
+        c->rn = renumber(*m, false);
+    }
     derive_kparams(c->params, c->dim, c->ps.kp);
     *rc = build_device(c.get(), m, d);
     if (*rc != MESO_OK) return nullptr;
@@ -496,7 +508,11 @@ int init_common(meso_ctx *c, const double *rho, const double *u, const double *T
     CUDA_TRY(cudaMemcpyAsync(c->ps.u, uu.data(), sizeof(double) * 3 * C, cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(cudaMemcpyAsync(c->ps.T, t.data(), sizeof(double) * C, cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(cudaMemcpyAsync(c->ps.q, qq.data(), sizeof(double) * 3 * C, cudaMemcpyHostToDevice, c->stream));
-    if (meso::plain_init(c->ps, mode, c->stream)) return fail(MESO_ERR_CUDA, "init kernel launch failed");
+    if (c->params.precision == MESO_FP32) {
+        if (meso::fp32_init(c->fs, mode, c->stream)) return fail(MESO_ERR_CUDA, "init kernel launch failed");
+    } else if (meso::plain_init(c->ps, mode, c->stream)) {
+        return fail(MESO_ERR_CUDA, "init kernel launch failed");
+    }
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     reset_status(c);
     c->step = 0;
@@ -547,7 +563,7 @@ extern "C" {
 
 const char *meso_last_error(void) { return last_error_cstr(); }
 
-const char *meso_version(void) { return "meso-gb300 1.0 sm_103a (FP64 plain step)"; }
+const char *meso_version(void) { return "meso-gb300 1.0 sm_103a (FP64 plain step, FP32 tiled Shakhov step)"; }
 
 int meso_case_load(const char *case_file, meso_case **out) {
     if (!case_file || !out) return fail(MESO_ERR_INVALID, "null argument");
@@ -658,6 +674,7 @@ void meso_ctx_destroy(meso_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    free_fp32_launch(c->fs, c->fs_owned);
     c->arena.release();
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -831,11 +848,16 @@ int meso_output(meso_ctx *c) {
     return MESO_OK;
 }
 
+// Bytes of the distribution state as stored on the device.
+static size_t state_bytes(const meso_ctx *c) {
+    if (c->params.precision == MESO_FP32) return sizeof(float2) * (size_t)c->C * c->f32.NVp;
+    const size_t nd = c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV ? 2 : 1;
+    return sizeof(double) * nd * (size_t)c->C * c->NV;
+}
+
 size_t meso_snapshot_size(meso_ctx *c) {
     if (!c) return 0;
-    const size_t cv = (size_t)c->C * c->NV;
-    const size_t nd = c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV ? 2 : 1;
-    return 64 + sizeof(double) * (nd * cv + 8 * (size_t)c->C) + sizeof(meso::DStatus);
+    return 64 + state_bytes(c) + sizeof(double) * 8 * (size_t)c->C + sizeof(meso::DStatus);
 }
 
 struct SnapHeader {
@@ -867,8 +889,13 @@ int meso_snapshot(meso_ctx *c, void *host, size_t bytes) {
         cudaMemcpyAsync(p, src, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
         p += n * sizeof(double);
     };
-    d2h(c->ps.f0, cv);
-    if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV) d2h(c->ps.f1, cv);
+    if (c->params.precision == MESO_FP32) {
+        cudaMemcpyAsync(p, c->f32.S[c->fs.cur], state_bytes(c), cudaMemcpyDeviceToHost, c->stream);
+        p += state_bytes(c);
+    } else {
+        d2h(c->ps.f0, cv);
+        if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV) d2h(c->ps.f1, cv);
+    }
     d2h(c->ps.rho, c->C);
     d2h(c->ps.u, 3 * (size_t)c->C);
     d2h(c->ps.T, c->C);
@@ -891,14 +918,27 @@ int meso_restore(meso_ctx *c, const void *host, size_t bytes) {
         cudaMemcpyAsync(dst, p, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
         p += n * sizeof(double);
     };
-    h2d(c->ps.f0, cv);
-    if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV) h2d(c->ps.f1, cv);
+    if (c->params.precision == MESO_FP32) {
+        cudaMemcpyAsync(c->f32.S[c->fs.cur], p, state_bytes(c), cudaMemcpyHostToDevice, c->stream);
+        p += state_bytes(c);
+    } else {
+        h2d(c->ps.f0, cv);
+        if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV) h2d(c->ps.f1, cv);
+    }
     h2d(c->ps.rho, c->C);
     h2d(c->ps.u, 3 * (size_t)c->C);
     h2d(c->ps.T, c->C);
     h2d(c->ps.q, 3 * (size_t)c->C);
     CUDA_TRY(cudaMemcpyAsync(c->d_status, p, sizeof(meso::DStatus), cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (c->params.precision == MESO_FP32) {
+        std::vector<double> uu(3 * (size_t)c->C);
+        std::vector<float2> u32(c->C);
+        cudaMemcpyAsync(uu.data(), c->ps.u, sizeof(double) * 3 * c->C, cudaMemcpyDeviceToHost, c->stream);
+        cudaStreamSynchronize(c->stream);
+        for (int i = 0; i < c->C; ++i) u32[i] = make_float2((float)uu[3 * i], (float)uu[3 * i + 1]);
+        cudaMemcpyAsync(c->f32.u32, u32.data(), sizeof(float2) * c->C, cudaMemcpyHostToDevice, c->stream);
+    }
     c->step = h.step;
     c->run_state = h.run_state;
     c->converged = h.converged;
@@ -913,6 +953,50 @@ int meso_restore(meso_ctx *c, const void *host, size_t bytes) {
 }
 
 size_t meso_ctx_device_bytes(meso_ctx *c) { return c ? c->arena.bytes : 0; }
+
+int meso_phase_times(meso_ctx *c, int32_t nsteps, double *ms, int32_t max_phases, int32_t *nphases) {
+    CTX_CHECK(c);
+    if (!c->initialized) return fail(MESO_ERR_INVALID, "meso_phase_times before initial()");
+    if (nsteps <= 0 || !ms) return fail(MESO_ERR_INVALID, "nsteps must be > 0 and ms non-null");
+    const bool f32 = c->params.precision == MESO_FP32;
+    const int np = f32 ? meso::F32_NPHASE : meso::PLAIN_NPHASE;
+    if (nphases) *nphases = np;
+    std::vector<cudaEvent_t> ev((size_t)np + 1);
+    for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
+    std::vector<double> acc(np, 0.0);
+    int rc = MESO_OK;
+    for (int s = 0; s < nsteps && c->run_state; ++s) {
+        rc = f32 ? meso::fp32_step(c->fs, c->stream, &c->last_launches, ev.data())
+                 : meso::plain_step(c->ps, c->stream, &c->last_launches, ev.data());
+        if (rc) {
+            rc = fail(MESO_ERR_CUDA, "kernel launch failed");
+            break;
+        }
+        if (cudaEventSynchronize(ev[np]) != cudaSuccess) {
+            rc = fail(MESO_ERR_CUDA, "phase timing failed");
+            break;
+        }
+        for (int k = 0; k < np; ++k) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            acc[k] += t;
+        }
+        c->solution_time += c->params.dt;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (rc) return rc;
+    rc = read_status(c);
+    if (rc) return rc;
+    c->step = c->h_status->step;
+    for (int k = 0; k < np && k < max_phases; ++k) ms[k] = acc[k] / nsteps;
+    return MESO_OK;
+}
+
+const char *meso_phase_name(meso_ctx *c, int32_t i) {
+    if (!c) return "";
+    if (c->params.precision == MESO_FP32) return (i >= 0 && i < meso::F32_NPHASE) ? meso::kFp32Phases[i] : "";
+    return (i >= 0 && i < meso::PLAIN_NPHASE) ? meso::kPlainPhases[i] : "";
+}
 
 double meso_last_step_ms(meso_ctx *c) { return c ? c->last_ms : 0.0; }
 

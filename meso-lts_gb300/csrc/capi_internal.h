@@ -4,12 +4,14 @@
 #include <cuda_runtime.h>
 
 #include <ctime>
+#include <new>
 #include <memory>
 #include <string>
 #include <vector>
 
 #include "host/case.h"
 #include "host/renumber.h"
+#include "host/tiles.h"
 #include "kernels/fp32_step.h"
 #include "kernels/plain_fp64.h"
 #include "meso_gpu.h"
@@ -20,7 +22,14 @@ namespace meso_host {
 struct DevArena {
     std::vector<void *> ptrs;
     size_t bytes = 0;
-    template <class T> T *alloc(size_t n);
+    template <class T> T *alloc(size_t n) {
+        if (n == 0) n = 1;
+        void *p = nullptr;
+        if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) throw std::bad_alloc();
+        ptrs.push_back(p);
+        bytes += n * sizeof(T);
+        return static_cast<T *>(p);
+    }
     void release();
     ~DevArena() { release(); }
 };
@@ -52,7 +61,10 @@ struct meso_ctx {
     meso::DStatus *d_status = nullptr;
     meso::DStatus *h_status = nullptr;  // pinned mirror
     meso::PlainState ps{};
-    meso::Fp32State fs{};
+    meso::F32Inst f32{};               // FP32 instance (device pointers), when precision == MESO_FP32
+    meso::Fp32State fs{};              // its single-instance launch state
+    std::vector<void *> fs_owned;
+    meso_host::TilePlan plan;
 
     // host step state (the reference's step / solution_time / run_state / converge_state)
     int step = 0;

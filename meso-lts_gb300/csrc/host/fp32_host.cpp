@@ -1,0 +1,240 @@
+// FP32 instance set-up.  See fp32_host.h.
+#include "fp32_host.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "capi_internal.h"
+
+namespace meso_host {
+
+bool plan_fp32(const meso_mesh_desc &m, int tile_cells, Renumbering &rn, TilePlan &plan) {
+    for (int T = std::min(tile_cells, meso::F32_MAX_CELLS); T >= 4; T = T * 3 / 4) {
+        std::vector<int> sizes;
+        rn = renumber_tiled(m, T, sizes);
+        if (build_tile_plan(m, rn, sizes, meso::F32_MAX_SLOTS, meso::F32_MAX_GSLOTS, meso::F32_MAX_OWNED,
+                            meso::F32_MAX_CELLS, plan))
+            return true;
+    }
+    return false;
+}
+
+int default_ngroup(int ntile, int chunks, int num_sms) {
+    // enough (tile, group) items for ~4 resident CTAs per SM, groups of at least 2 chunks
+    int want = (4 * num_sms + ntile - 1) / std::max(ntile, 1);
+    want = std::max(1, std::min(want, std::max(1, chunks / 2)));
+    return want;
+}
+
+namespace {
+template <class T> T *up(DevArena &A, const std::vector<T> &v, cudaStream_t s) {
+    T *p = A.alloc<T>(v.size());
+    if (!v.empty()) cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+    return p;
+}
+}  // namespace
+
+int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d, const TilePlan &P, int ngroup) {
+    auto &A = c->arena;
+    auto s = c->stream;
+    const int C = m->ncell, F = m->nface, NV = d->nv;
+    const int NVp = (NV + 31) / 32 * 32;
+    const auto &rn = c->rn;
+    meso::F32Inst I;
+    std::memset(&I, 0, sizeof(I));
+    I.C = C;
+    I.F = F;
+    I.NV = NV;
+    I.NVp = NVp;
+    I.ntile = P.ntile;
+    I.chunks = NVp / 32;
+    I.ngroup = ngroup > 0 ? std::min(ngroup, I.chunks) : default_ngroup(P.ntile, I.chunks, c->num_sms);
+    const meso_params &p = c->params;
+    I.dt = p.dt;
+    I.hdt = p.dt * 0.5;
+    I.R = p.R;
+    I.Pr = p.Pr;
+    I.mu0 = p.mu0;
+    I.vhs = p.vhs_index;
+    I.T0 = p.T0;
+    I.Kd = (double)p.K;
+    I.Cv = (p.K + 3.0) * p.R * 0.5;
+    I.gamma = (p.K + 5.0) / (p.K + 3.0);
+    I.gradient = p.gradient_switch;
+    // renumbered face geometry and boundary index
+    std::vector<int> fown(F), fnei(F), fbnd(F, -1), bface, fmark(F);
+    std::vector<float2> fn32(F), fdo(F), fdn(F);
+    std::vector<double2> fn64(F);
+    std::vector<float> farea(F);
+    std::vector<double> farea64(F);
+    for (int f = 0; f < F; ++f) {
+        int o = rn.face_new2old[f];
+        int ow = m->face_cell[2 * o], ne = m->face_cell[2 * o + 1];
+        fown[f] = rn.cell_old2new[ow];
+        fnei[f] = rn.cell_old2new[ne];
+        fmark[f] = m->face_mark[o];
+        const double *n = m->face_normal + 3 * (size_t)o, *fp = m->face_pos + 3 * (size_t)o;
+        fn64[f] = make_double2(n[0], n[1]);
+        fn32[f] = make_float2((float)n[0], (float)n[1]);
+        const double *po = m->cell_pos + 3 * (size_t)ow, *pn = m->cell_pos + 3 * (size_t)ne;
+        fdo[f] = make_float2((float)(fp[0] - po[0]), (float)(fp[1] - po[1]));
+        fdn[f] = make_float2((float)(fp[0] - pn[0]), (float)(fp[1] - pn[1]));
+        farea[f] = (float)m->face_area[o];
+        farea64[f] = m->face_area[o];
+        if (c->marks[fmark[f]].type != MESO_BC_FLUID_INTERIOR) {
+            fbnd[f] = (int)bface.size();
+            bface.push_back(f);
+        }
+    }
+    I.nb = (int)bface.size();
+    std::vector<float> xx(NVp, 0.f), xy(NVp, 0.f), w(NVp, 0.f);
+    std::vector<double> xx64(NVp, 0.0), xy64(NVp, 0.0), w64(NVp, 0.0);
+    for (int q = 0; q < NV; ++q) {
+        xx64[q] = d->xi[3 * q];
+        xy64[q] = d->xi[3 * q + 1];
+        w64[q] = d->w[q];
+        xx[q] = (float)xx64[q];
+        xy[q] = (float)xy64[q];
+        w[q] = (float)w64[q];
+    }
+    std::vector<int> sym(3 * (size_t)NV, 0);
+    if (d->sym)
+        for (int q = 0; q < 3 * NV; ++q) sym[q] = d->sym[q];
+    try {
+        I.tile_cstart = up(A, P.tile_cstart, s);
+        I.tile_ncell = up(A, P.tile_ncell, s);
+        I.tile_slot_ptr = up(A, P.tile_slot_ptr, s);
+        I.slot_cell = up(A, P.slot_cell, s);
+        I.tile_gslots = up(A, P.tile_gslots, s);
+        I.tile_gsp_off = up(A, P.tile_gsp_off, s);
+        I.gs_ptr = up(A, P.gs_ptr, s);
+        I.gs_nbr = up(A, P.gs_nbr, s);
+        I.gs_ax = up(A, P.gs_ax, s);
+        I.gs_ay = up(A, P.gs_ay, s);
+        I.tile_fstart = up(A, P.tile_fstart, s);
+        I.face_own_slot = up(A, P.face_own_slot, s);
+        I.face_nei_slot = up(A, P.face_nei_slot, s);
+        I.cf_oslot = up(A, P.cf_oslot, s);
+        I.cf_ptr = c->dm.cf_ptr;
+        I.cf_face = c->dm.cf_face;
+        I.fown = up(A, fown, s);
+        I.fnei = up(A, fnei, s);
+        I.fbnd = up(A, fbnd, s);
+        I.bface = up(A, bface, s);
+        I.fmark = up(A, fmark, s);
+        I.fn32 = up(A, fn32, s);
+        I.fdo = up(A, fdo, s);
+        I.fdn = up(A, fdn, s);
+        I.fn64 = up(A, fn64, s);
+        I.farea = up(A, farea, s);
+        I.farea64 = up(A, farea64, s);
+        I.vol = c->dm.vol;
+        I.marks = c->dm.marks;
+        I.mask = c->dm.mask;
+        I.cn_ptr = c->dm.cn_ptr;
+        I.cn_cell = c->dm.cn_cell;
+        I.lsq_dr = c->dm.lsq_dr;
+        I.xi32x = up(A, xx, s);
+        I.xi32y = up(A, xy, s);
+        I.w32 = up(A, w, s);
+        I.xi64x = up(A, xx64, s);
+        I.xi64y = up(A, xy64, s);
+        I.w64 = up(A, w64, s);
+        I.sym = up(A, sym, s);
+        const size_t cv = (size_t)C * NVp;
+        I.S[0] = A.alloc<float2>(cv);
+        I.S[1] = A.alloc<float2>(cv);
+        I.fpart = A.alloc<double>((size_t)I.ngroup * F * meso::F32_NMOM);
+        I.u32 = A.alloc<float2>(C);
+        I.fk = A.alloc<meso::FaceK>(F);
+        I.fmac = A.alloc<double>((size_t)F * 8);
+        I.fgbar = A.alloc<double>((size_t)F * 4);
+        I.fsum = A.alloc<double>((size_t)F * 4);
+        I.bnd_in = A.alloc<float2>((size_t)std::max(I.nb, 1) * NVp);
+        I.bnd_out = A.alloc<float2>((size_t)std::max(I.nb, 1) * NVp);
+        I.ck = A.alloc<meso::CellK>(C);
+        I.qpart = A.alloc<double>((size_t)I.ngroup * C * 2);
+        I.rho = A.alloc<double>(C);
+        I.u = A.alloc<double>(3 * (size_t)C);
+        I.T = A.alloc<double>(C);
+        I.q = A.alloc<double>(3 * (size_t)C);
+        I.fm0 = A.alloc<double>(C);
+        I.fm1 = A.alloc<double>(3 * (size_t)C);
+        I.fm2 = A.alloc<double>(C);
+        I.repair_list = A.alloc<int>(C);
+        I.status = c->d_status;
+        cudaMemsetAsync(I.S[0], 0, cv * sizeof(float2), s);
+        cudaMemsetAsync(I.S[1], 0, cv * sizeof(float2), s);
+        cudaMemsetAsync(I.fm0, 0, sizeof(double) * C, s);
+        cudaMemsetAsync(I.fm1, 0, sizeof(double) * 3 * C, s);
+        cudaMemsetAsync(I.fm2, 0, sizeof(double) * C, s);
+    } catch (const std::bad_alloc &) {
+        cudaGetLastError();
+        return fail(MESO_ERR_OOM, "device allocation failed for the FP32 state");
+    }
+    c->f32 = I;
+    // the plain-state macro pointers alias the FP32 instance so the shared read-back paths work
+    c->ps.rho = I.rho;
+    c->ps.u = I.u;
+    c->ps.T = I.T;
+    c->ps.q = I.q;
+    c->ps.fm0 = I.fm0;
+    c->ps.fm1 = I.fm1;
+    c->ps.fm2 = I.fm2;
+    std::vector<meso::F32Inst> one(1, I);
+    c->fs.cur = 0;
+    if (build_fp32_launch(one, c->num_sms, c->fs, c->fs_owned)) return fail(MESO_ERR_OOM, "launch state allocation failed");
+    cudaStreamSynchronize(s);
+    return MESO_OK;
+}
+
+int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso::Fp32State &s,
+                      std::vector<void *> &owned) {
+    const int n = (int)insts.size();
+    std::vector<int2> items;
+    std::vector<int> foff(1, 0), coff(1, 0), boff(1, 0);
+    for (int i = 0; i < n; ++i) {
+        const auto &I = insts[i];
+        for (int t = 0; t < I.ntile; ++t)
+            for (int g = 0; g < I.ngroup; ++g) items.push_back(make_int2(i, t * I.ngroup + g));
+        foff.push_back(foff.back() + I.F);
+        coff.push_back(coff.back() + I.C);
+        boff.push_back(boff.back() + I.nb);
+    }
+    // largest work first: items of big-NV instances lead the list (persistent CTAs take them in order)
+    std::stable_sort(items.begin(), items.end(), [&](const int2 &a, const int2 &b) {
+        const auto &A = insts[a.x], &B = insts[b.x];
+        long wa = (long)((A.chunks + A.ngroup - 1) / A.ngroup), wb = (long)((B.chunks + B.ngroup - 1) / B.ngroup);
+        return wa > wb;
+    });
+    auto put = [&](const void *src, size_t bytes) -> void * {
+        void *p = nullptr;
+        if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) return nullptr;
+        owned.push_back(p);
+        cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+        return p;
+    };
+    s.d_inst = (meso::F32Inst *)put(insts.data(), sizeof(meso::F32Inst) * n);
+    s.d_items = (int2 *)put(items.data(), sizeof(int2) * items.size());
+    s.d_face_items = (int *)put(foff.data(), sizeof(int) * foff.size());
+    s.d_cell_items = (int *)put(coff.data(), sizeof(int) * coff.size());
+    s.d_bnd_items = (int *)put(boff.data(), sizeof(int) * boff.size());
+    if (!s.d_inst || !s.d_items || !s.d_face_items || !s.d_cell_items || !s.d_bnd_items) return -1;
+    s.ninst = n;
+    s.nitems = (int)items.size();
+    s.total_faces = foff.back();
+    s.total_cells = coff.back();
+    s.total_bnd = boff.back();
+    s.num_sms = num_sms;
+    s.enabled = 1;
+    return 0;
+}
+
+void free_fp32_launch(meso::Fp32State &s, std::vector<void *> &owned) {
+    for (void *p : owned) cudaFree(p);
+    owned.clear();
+    s = meso::Fp32State();
+}
+
+}  // namespace meso_host

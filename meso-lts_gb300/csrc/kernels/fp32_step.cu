@@ -1,0 +1,895 @@
+// FP32-storage Shakhov CDUGKS step (2-D), tiled and fused.
+//
+// Storage: g, h interleaved as float2, velocity-contiguous per cell
+// ([cell][NVp], NVp = NV rounded up to 32), two buffers (state n, n+1).
+// A step is seven launches, each over all instances of a batch:
+//
+//   P1  k32_moments      per (tile, velocity group) CTA: stage the tile and its
+//                        two-ring halo for 32 velocities in shared memory,
+//                        compute every tile / 1-ring cell's least-squares
+//                        gradient once, reconstruct each owned face (half-step
+//                        upwind, cdugks_shakhov.cpp:223-276) and accumulate 11
+//                        raw moments about a reference velocity (FP32 terms,
+//                        warp sums, compensated FP32 across chunks, FP64
+//                        partial per group)
+//   FMa k32_face_macros  one thread per face, FP64: face rho, u, T, tau, q
+//                        (cdugks_shakhov.cpp:341-349) and the moment fluxes of
+//                        the reconstructed values, by exact algebra on the moments
+//   FMb k32_face_eqflux  one warp per interior face: discrete moment fluxes of
+//                        the face Shakhov equilibrium (FP32 terms, FP64 result)
+//   BND k32_boundary     one block per boundary face: blend, diffuse-wall
+//                        balance, inlets / outlets, symmetry, slip
+//                        (cdugks_shakhov.cpp:364-607), moment fluxes
+//   CM  k32_cell_macros  one thread per cell, FP64: flux moments from the face
+//                        fluxes, conservative update, tau, evolution constants
+//                        (cdugks_shakhov.cpp:636-668), NaN / T<0 monitor
+//   P2  k32_update       per (tile, group) CTA: same staging and gradients, then
+//                        per cell and velocity: face values (reconstruction
+//                        blended with the face equilibrium, or the boundary
+//                        value), flux, evolution to f-bar-plus, heat-flux
+//                        partials (cdugks_shakhov.cpp:616-696)
+//   QR  k32_heat_flux    q = sum of the heat-flux partials (FP64)
+//
+// Face values never go to HBM except on boundary faces: the state is read
+// twice and written once per step.  Upwind classification is exact: n.xi is
+// evaluated in FP32 and re-evaluated in FP64 in the reference's order when it
+// lies within a rounding margin of zero.  Per-face and per-cell scalar work
+// (pow, divisions) runs one thread per face / cell in FP64.
+#include <cfloat>
+#include <climits>
+
+#include "fp32_step.h"
+
+namespace meso {
+namespace {
+
+constexpr int kT = F32_WARPS * 32;
+constexpr double kLOG2E = 1.4426950408889634;
+constexpr size_t kSmemBytes =
+    sizeof(float2) * F32_MAX_SLOTS * 32 + sizeof(float4) * F32_MAX_GSLOTS * 32 + sizeof(float) * F32_MAX_OWNED * 24;
+
+__device__ __forceinline__ float fast_ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// 0: from the owner (n0.xi >= VSMALL), 1: from the neighbour (< -VSMALL), 2: between.
+__device__ __forceinline__ int classify(const F32Inst &I, int f, int p, float d32, float xx, float xy) {
+    const float margin = 1e-5f * (fabsf(xx) + fabsf(xy));
+    if (d32 > margin) return 0;
+    if (d32 < -margin) return 1;
+    const double2 n = I.fn64[f];
+    const double d = __dadd_rn(__dmul_rn(n.x, I.xi64x[p]), __dmul_rn(n.y, I.xi64y[p]));
+    return d >= kVSMALL ? 0 : (d < -kVSMALL ? 1 : 2);
+}
+
+// Shakhov g and h at one velocity (2-D) from precomputed scalars (cdugks_shakhov.cpp:185-211).
+__device__ __forceinline__ float2 shakhov(float cx, float cy, float A, float bl, float qx, float qy, float sg,
+                                          float sh, float iRT, float hm, float k3, float twoK) {
+    const float cc = fmaf(cx, cx, cy * cy);
+    const float cq = fmaf(cx, qx, cy * qy);
+    const float gm = A * fast_ex2(-cc * bl);
+    const float t = cc * iRT;
+    const float g = gm * fmaf(sg * cq, t - 4.0f, 1.0f);
+    const float h = gm * fmaf(sh * cq, fmaf(t - 2.0f, k3, -twoK), hm);
+    return make_float2(g, h);
+}
+
+__device__ __forceinline__ void kahan(float &s, float &c, float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+template <int N> __device__ __forceinline__ void warp_sum(float (&v)[N]) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < N; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+}
+
+template <int N> __device__ __forceinline__ float pick(const float (&v)[N], int lane) {
+    float r = 0.f;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r = (lane == k) ? v[k] : r;
+    return r;
+}
+
+// instance owning global index g, given prefix offsets off[0..n]
+__device__ __forceinline__ int find_inst(const int *off, int n, int g) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (off[mid] <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+struct Smem {
+    float2 *phi;  // [F32_MAX_SLOTS][32]
+    float4 *G;    // [F32_MAX_GSLOTS][32]
+    float *acc;   // compensated accumulators (per owned face or per cell)
+};
+
+__device__ __forceinline__ Smem smem_layout(float4 *base) {
+    Smem s;
+    s.phi = reinterpret_cast<float2 *>(base);
+    s.G = reinterpret_cast<float4 *>(s.phi + F32_MAX_SLOTS * 32);
+    s.acc = reinterpret_cast<float *>(s.G + F32_MAX_GSLOTS * 32);
+    return s;
+}
+
+// Stage the tile's slots for one chunk and compute the gradients of the first nG slots.
+__device__ __forceinline__ void stage_chunk(const F32Inst &I, const float2 *__restrict__ S, int tile, int p,
+                                            const Smem &sm) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sbase = I.tile_slot_ptr[tile];
+    const int nS = I.tile_slot_ptr[tile + 1] - sbase;
+    const int nG = I.tile_gslots[tile];
+    const size_t NVp = (size_t)I.NVp;
+    for (int s = warp; s < nS; s += F32_WARPS) sm.phi[s * 32 + lane] = __ldg(S + (size_t)I.slot_cell[sbase + s] * NVp + p);
+    __syncthreads();
+    if (I.gradient) {
+        const int *gp = I.gs_ptr + I.tile_gsp_off[tile];
+        for (int s = warp; s < nG; s += F32_WARPS) {
+            const float2 c = sm.phi[s * 32 + lane];
+            float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int j = gp[s]; j < gp[s + 1]; ++j) {
+                const float2 v = sm.phi[I.gs_nbr[j] * 32 + lane];
+                const float ax = I.gs_ax[j], ay = I.gs_ay[j];
+                const float dg = v.x - c.x, dh = v.y - c.y;
+                g.x = fmaf(ax, dg, g.x);
+                g.y = fmaf(ay, dg, g.y);
+                g.z = fmaf(ax, dh, g.z);
+                g.w = fmaf(ay, dh, g.w);
+            }
+            sm.G[s * 32 + lane] = g;
+        }
+    } else {
+        for (int s = warp; s < nG; s += F32_WARPS) sm.G[s * 32 + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+}
+
+// Half-step reconstruction from slot s: phi + (d - xi dt/2) . grad   (g and h)
+__device__ __forceinline__ float2 recon(const Smem &sm, int s, float2 d, float hx, float hy) {
+    const int lane = threadIdx.x & 31;
+    const float2 v = sm.phi[s * 32 + lane];
+    const float4 g = sm.G[s * 32 + lane];
+    const float ax = d.x - hx, ay = d.y - hy;
+    return make_float2(fmaf(ax, g.x, fmaf(ay, g.y, v.x)), fmaf(ax, g.z, fmaf(ay, g.w, v.y)));
+}
+
+// Face value from the upwind side(s), gradient off: plain upwind (cdugks_shakhov.cpp:277-298).
+__device__ __forceinline__ float2 face_bar(const F32Inst &I, const Smem &sm, int f, int cls, int os, int ns, float hx,
+                                           float hy) {
+    if (cls == 0) return recon(sm, os, I.fdo[f], hx, hy);
+    if (cls == 1) return recon(sm, ns, I.fdn[f], hx, hy);
+    const float2 a = recon(sm, os, I.fdo[f], hx, hy), b = recon(sm, ns, I.fdn[f], hx, hy);
+    return make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
+}
+
+// =============================================================================
+// P1: raw face moments
+// =============================================================================
+__global__ void __launch_bounds__(kT, 2) k32_moments(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
+                                                    int nitems, int cur) {
+    extern __shared__ float4 smem_raw[];
+    const Smem sm = smem_layout(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int2 item = items[it];
+        const F32Inst &I = insts[item.x];
+        if (step_stopped(I.status)) continue;
+        const int tile = item.y / I.ngroup, grp = item.y % I.ngroup;
+        const int fs = I.tile_fstart[tile], nOF = I.tile_fstart[tile + 1] - fs;
+        const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
+        const int ch0 = grp * cpg, ch1 = min(I.chunks, ch0 + cpg);
+        const float2 *S = I.S[cur];
+        const float hdt = (float)I.hdt;
+        for (int k = threadIdx.x; k < nOF * 22; k += kT) sm.acc[k] = 0.f;
+        for (int ch = ch0; ch < ch1; ++ch) {
+            const int p = ch * 32 + lane;
+            stage_chunk(I, S, tile, p, sm);
+            const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
+            const float hx = hdt * xx, hy = hdt * xy;
+            for (int fl = warp; fl < nOF; fl += F32_WARPS) {
+                const int f = fs + fl;
+                const int os = I.face_own_slot[f], ns = I.face_nei_slot[f];
+                const float2 n = I.fn32[f];
+                const int cls = classify(I, f, p, fmaf(n.x, xx, n.y * xy), xx, xy);
+                const float2 gb = face_bar(I, sm, f, cls, os, ns, hx, hy);
+                const int b = I.fbnd[f];
+                if (b >= 0) I.bnd_in[(size_t)b * I.NVp + p] = gb;
+                const float2 uo = I.u32[I.fown[f]], un = I.u32[I.fnei[f]];
+                const float c0x = xx - 0.5f * (uo.x + un.x), c0y = xy - 0.5f * (uo.y + un.y);
+                const float wg = w * gb.x, wh = w * gb.y;
+                const float cc = fmaf(c0x, c0x, c0y * c0y);
+                float m[F32_NMOM] = {wg,           c0x * wg,      c0y * wg,      c0x * c0x * wg,
+                                     c0x * c0y * wg, c0y * c0y * wg, c0x * cc * wg, c0y * cc * wg,
+                                     wh,           c0x * wh,      c0y * wh};
+                warp_sum(m);
+                if (lane < F32_NMOM) {
+                    float *a = sm.acc + fl * 22 + 2 * lane;
+                    kahan(a[0], a[1], pick(m, lane));
+                }
+            }
+            __syncthreads();
+        }
+        double *out = I.fpart + ((size_t)grp * I.F + fs) * F32_NMOM;
+        for (int k = threadIdx.x; k < nOF * F32_NMOM; k += kT)
+            out[k] = (double)sm.acc[2 * k] - (double)sm.acc[2 * k + 1];
+        __syncthreads();
+    }
+}
+
+// =============================================================================
+// FMa: face macros from the raw moments (one thread per face, FP64)
+// =============================================================================
+__global__ void k32_face_macros(const F32Inst *__restrict__ insts, const int *__restrict__ foff, int ninst,
+                                int total) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int i = find_inst(foff, ninst, g);
+        const F32Inst &I = insts[i];
+        if (step_stopped(I.status)) continue;
+        const int f = g - foff[i];
+        double M[F32_NMOM];
+        for (int k = 0; k < F32_NMOM; ++k) M[k] = 0.0;
+        for (int grp = 0; grp < I.ngroup; ++grp) {
+            const double *pp = I.fpart + ((size_t)grp * I.F + f) * F32_NMOM;
+            for (int k = 0; k < F32_NMOM; ++k) M[k] += pp[k];
+        }
+        const float2 uo = I.u32[I.fown[f]], un = I.u32[I.fnei[f]];
+        const double u0x = (double)(0.5f * (uo.x + un.x)), u0y = (double)(0.5f * (uo.y + un.y));
+        const double rho = M[0];
+        const double dx = M[1] / rho, dy = M[2] / rho;
+        const double ux = u0x + dx, uy = u0y + dy;
+        const double trM = M[3] + M[5];
+        const double dd = dx * dx + dy * dy;
+        const double e2 = trM - rho * dd + M[8];  // sum w (|xi-u|^2 g + h)
+        const double T = (0.5 * e2 / rho) / I.Cv;
+        const double tau = I.mu0 * pow(T / I.T0, I.vhs) / (rho * I.R * T);
+        const double m3x = M[6] - 2.0 * (M[3] * dx + M[4] * dy) - dx * trM + 2.0 * dd * rho * dx + M[9] - dx * M[8];
+        const double m3y = M[7] - 2.0 * (M[4] * dx + M[5] * dy) - dy * trM + 2.0 * dd * rho * dy + M[10] - dy * M[8];
+        const double qs = tau / (2.0 * tau + I.hdt * I.Pr);
+        const double qx = qs * m3x, qy = qs * m3y;
+        const double Cs = I.hdt / (2.0 * tau + I.hdt);
+        double *fm = I.fmac + (size_t)f * 8;
+        fm[0] = rho;
+        fm[1] = ux;
+        fm[2] = uy;
+        fm[3] = T;
+        fm[4] = qx;
+        fm[5] = qy;
+        fm[6] = Cs;
+        fm[7] = tau;
+        const double RT = I.R * T, p = rho * RT;
+        FaceK k;
+        k.ux = (float)ux;
+        k.uy = (float)uy;
+        k.qx = (float)qx;
+        k.qy = (float)qy;
+        k.A = (float)(rho / (2.0 * kPI * RT));
+        k.bl = (float)(kLOG2E / (2.0 * RT));
+        k.sg = (float)((1.0 - I.Pr) / (5.0 * p * RT));
+        k.sh = (float)((1.0 - I.Pr) / (5.0 * p));
+        k.iRT = (float)(1.0 / RT);
+        k.hm = (float)((I.Kd + 1.0) * RT);
+        k.Cs = (float)Cs;
+        k.oCs = (float)(1.0 - Cs);
+        I.fk[f] = k;
+        // moment fluxes of the reconstructed values along n0 (per unit area)
+        const double2 n = I.fn64[f];
+        const double un0 = u0x * n.x + u0y * n.y;
+        const double M1n = M[1] * n.x + M[2] * n.y;
+        const double M2nx = M[3] * n.x + M[4] * n.y, M2ny = M[4] * n.x + M[5] * n.y;
+        const double uu0 = u0x * u0x + u0y * u0y;
+        double *fb = I.fgbar + (size_t)f * 4;
+        fb[0] = un0 * M[0] + M1n;
+        fb[1] = u0x * un0 * M[0] + u0x * M1n + un0 * M[1] + M2nx;
+        fb[2] = u0y * un0 * M[0] + u0y * M1n + un0 * M[2] + M2ny;
+        fb[3] = un0 * (uu0 * M[0] + 2.0 * (u0x * M[1] + u0y * M[2]) + trM) + uu0 * M1n +
+                2.0 * (u0x * M2nx + u0y * M2ny) + (M[6] * n.x + M[7] * n.y) + un0 * M[8] + (M[9] * n.x + M[10] * n.y);
+    }
+}
+
+// =============================================================================
+// FMb: discrete moment fluxes of the face equilibrium (one warp per interior face)
+// =============================================================================
+__global__ void __launch_bounds__(256) k32_face_eqflux(const F32Inst *__restrict__ insts, const int *__restrict__ foff,
+                                                      int ninst, int total) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
+        const int i = find_inst(foff, ninst, g);
+        const F32Inst &I = insts[i];
+        if (step_stopped(I.status)) continue;
+        const int f = g - foff[i];
+        if (I.fbnd[f] >= 0) continue;
+        const FaceK k = I.fk[f];
+        const float2 n = I.fn32[f];
+        const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
+        float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int p = lane; p < I.NVp; p += 32) {
+            const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
+            const float2 gs = shakhov(xx - k.ux, xy - k.uy, k.A, k.bl, k.qx, k.qy, k.sg, k.sh, k.iRT, k.hm, k3, twoK);
+            const float wkn = w * fmaf(n.x, xx, n.y * xy);
+            const float a = wkn * gs.x;
+            kahan(s[0], c[0], a);
+            kahan(s[1], c[1], a * xx);
+            kahan(s[2], c[2], a * xy);
+            kahan(s[3], c[3], wkn * fmaf(fmaf(xx, xx, xy * xy), gs.x, gs.y));
+        }
+        float v[4] = {s[0] - c[0], s[1] - c[1], s[2] - c[2], s[3] - c[3]};
+        warp_sum(v);
+        if (lane == 0) {
+            double *o = I.fsum + (size_t)f * 4;
+            o[0] = v[0];
+            o[1] = v[1];
+            o[2] = v[2];
+            o[3] = v[3];
+        }
+    }
+}
+
+// =============================================================================
+// BND: boundary faces (one block per face); cdugks_shakhov.cpp:364-607
+// =============================================================================
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sh[k];
+    __syncthreads();
+    return s;
+}
+
+__device__ __forceinline__ double solve_pressure(double P0, double R, double T, double ux, double uy, double gamma) {
+    const double Ma = sqrt(ux * ux + uy * uy) / sqrt(gamma * R * T);
+    return P0 / pow(1.0 + (gamma - 1.0) / 2.0 * (Ma * Ma), gamma / (gamma - 1.0));
+}
+
+__global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ insts, const int *__restrict__ boff,
+                                                   int ninst, int total) {
+    __shared__ double sh[8];
+    for (int g = blockIdx.x; g < total; g += gridDim.x) {
+        const int i = find_inst(boff, ninst, g);
+        const F32Inst &I = insts[i];
+        if (step_stopped(I.status)) continue;
+        const int b = g - boff[i];
+        const int f = I.bface[b];
+        const meso_mark_desc mk = I.marks[I.fmark[f]];
+        const int nb = I.fown[f];
+        const FaceK k = I.fk[f];
+        const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
+        float2 *bin = I.bnd_in + (size_t)b * I.NVp;
+        float2 *bout = I.bnd_out + (size_t)b * I.NVp;
+        const float2 n = I.fn32[f];
+        // blend with the face equilibrium (cdugks_shakhov.cpp:350-361)
+        for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
+            const float xx = I.xi32x[p], xy = I.xi32y[p];
+            const float2 gs = shakhov(xx - k.ux, xy - k.uy, k.A, k.bl, k.qx, k.qy, k.sg, k.sh, k.iRT, k.hm, k3, twoK);
+            const float2 gb = bin[p];
+            bin[p] = make_float2(fmaf(k.oCs, gb.x, k.Cs * gs.x), fmaf(k.oCs, gb.y, k.Cs * gs.y));
+        }
+        __syncthreads();
+        // incoming set for this face type; kn = xi . n_in = -(xi . n0): class 1 = incoming, 2 = grazing
+        const int type = mk.type;
+        double rr = 0.0, TT = 0.0, uux = 0.0, uuy = 0.0;
+        int mode = 0;  // 0 keep, 1 Maxwell incoming, 2 wall, 3 slip wall, 4 symmetry
+        if (type == MESO_BC_PRESSURE_INLET) {
+            const double T_m = I.T[nb], umx = I.u[3 * nb], umy = I.u[3 * nb + 1];
+            const double nx = -(double)I.fn64[f].x, ny = -(double)I.fn64[f].y;
+            const double s = umx * nx + umy * ny;
+            uux = nx * s;
+            uuy = ny * s;
+            TT = mk.temperature;
+            rr = solve_pressure(mk.pressure, I.R, T_m, uux, uuy, I.gamma) / (I.R * TT);
+            mode = 1;
+        } else if (type == MESO_BC_FARFIELD_INLET) {
+            rr = mk.density;
+            uux = mk.velocity[0];
+            uuy = mk.velocity[1];
+            TT = mk.temperature;
+            mode = 1;
+        } else if (type == MESO_BC_FREESTREAM_INLET) {
+            TT = mk.temperature;
+            rr = mk.pressure / (I.R * TT);
+            uux = mk.velocity[0];
+            uuy = mk.velocity[1];
+            mode = 1;
+        } else if (type == MESO_BC_PRESSURE_OUTLET) {
+            const double umx = I.u[3 * nb], umy = I.u[3 * nb + 1], T_m = I.T[nb];
+            rr = solve_pressure(mk.pressure, I.R, T_m, umx, umy, I.gamma) / (I.R * T_m);
+            const double nx = (double)I.fn64[f].x, ny = (double)I.fn64[f].y;  // nv_e = -nv = n0
+            const double s = umx * nx + umy * ny;
+            uux = nx * s;
+            uuy = ny * s;
+            TT = mk.temperature;
+            mode = 1;
+        } else if (type == MESO_BC_FARFIELD_OUTLET) {
+            rr = I.rho[nb];
+            TT = I.T[nb];
+            uux = I.u[3 * nb];
+            uuy = I.u[3 * nb + 1];
+            mode = 1;
+        } else if (type == MESO_BC_WALL) {
+            mode = 2;
+        } else if (type == MESO_BC_SLIP_WALL) {
+            mode = 3;
+        } else if (type == MESO_BC_SYMMETRY) {
+            mode = 4;
+        }
+        double rho_w = 0.0;
+        if (mode == 2 || mode == 3) {
+            double T_w = 0.0;
+            if (mk.temperature_type == MESO_PATCH_ZERO_GRADIENT) T_w = I.T[nb];
+            else if (mk.temperature_type == MESO_PATCH_FIXED_VALUE) T_w = mk.temperature;
+            const double RTw = I.R * T_w;
+            const float Aw = (float)(1.0 / (2.0 * kPI * RTw)), blw = (float)(kLOG2E / (2.0 * RTw));
+            const float uwx = (float)mk.velocity[0], uwy = (float)mk.velocity[1];
+            float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+            for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
+                const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
+                const float d = fmaf(n.x, xx, n.y * xy);
+                const int cls = classify(I, f, p, d, xx, xy);
+                const float kn = -d;
+                if (cls == 1) {  // kn >= VSMALL
+                    const float cx = xx - uwx, cy = xy - uwy;
+                    kahan(s1, c1, kn * w * Aw * fast_ex2(-fmaf(cx, cx, cy * cy) * blw));
+                } else {
+                    kahan(s0, c0, -kn * w * bin[p].x);
+                }
+            }
+            const double num = block_sum((double)s0 - (double)c0, sh);
+            const double den = block_sum((double)s1 - (double)c1, sh);
+            rho_w = num / den;
+            rr = rho_w;
+            TT = mk.temperature;
+            uux = mk.velocity[0];
+            uuy = mk.velocity[1];
+        }
+        const double RT = I.R * TT;
+        const float A = (float)(rr / (2.0 * kPI * RT)), bl = (float)(kLOG2E / (2.0 * RT)), hm = (float)((I.Kd + 1.0) * RT);
+        const float ux = (float)uux, uy = (float)uuy;
+        const int dir = mk.direction;
+        const float au = (float)mk.alpha_u, aT = (float)mk.alpha_T;
+        float s[4] = {0.f, 0.f, 0.f, 0.f}, cc4[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
+            const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
+            const float d = fmaf(n.x, xx, n.y * xy);
+            float2 v = bin[p];
+            if (mode != 0 && p < I.NV) {
+                const int cls = classify(I, f, p, d, xx, xy);
+                if (mode == 4) {
+                    const float2 r = bin[I.sym[3 * p + dir]];
+                    if (cls == 1) v = r;
+                    else if (cls == 2) v = make_float2(0.5f * (v.x + r.x), 0.5f * (v.y + r.y));
+                } else if (cls != 0) {
+                    const float cx = xx - ux, cy = xy - uy;
+                    const float gm = A * fast_ex2(-fmaf(cx, cx, cy * cy) * bl);
+                    float2 inc = make_float2(gm, hm * gm);
+                    if (mode == 3) {
+                        const float2 r = bin[I.sym[3 * p + dir]];
+                        inc = make_float2((1.f - au) * inc.x + au * r.x, (1.f - aT) * inc.y + aT * r.y);
+                    }
+                    if (mode == 1) {
+                        if (cls == 1) v = inc;
+                    } else {
+                        v = cls == 1 ? inc : make_float2(0.5f * (inc.x + v.x), 0.5f * (inc.y + v.y));
+                    }
+                }
+            }
+            bout[p] = v;
+            // moment fluxes of the final face values along n0
+            const float wkn = w * d;
+            const float a = wkn * v.x;
+            kahan(s[0], cc4[0], a);
+            kahan(s[1], cc4[1], a * xx);
+            kahan(s[2], cc4[2], a * xy);
+            kahan(s[3], cc4[3], wkn * fmaf(fmaf(xx, xx, xy * xy), v.x, v.y));
+        }
+        double tot[4];
+        for (int q = 0; q < 4; ++q) tot[q] = block_sum((double)s[q] - (double)cc4[q], sh);
+        if (threadIdx.x == 0) {
+            double *o = I.fsum + (size_t)f * 4;
+            for (int q = 0; q < 4; ++q) o[q] = tot[q];
+        }
+        __syncthreads();
+    }
+}
+
+// =============================================================================
+// CM: cell macros and evolution constants (one thread per cell, FP64)
+// =============================================================================
+__device__ __forceinline__ double tau_f(const F32Inst &I, double rho, double t) {
+    return I.mu0 * pow(t / I.T0, I.vhs) / (rho * I.R * t);
+}
+
+__global__ void k32_cell_macros(const F32Inst *__restrict__ insts, const int *__restrict__ coff, int ninst, int total) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int i = find_inst(coff, ninst, g);
+        const F32Inst &I = insts[i];
+        if (step_stopped(I.status)) continue;
+        const int c = g - coff[i];
+        double m0 = 0.0, m1x = 0.0, m1y = 0.0, m2 = 0.0;
+        for (int j = I.cf_ptr[c]; j < I.cf_ptr[c + 1]; ++j) {
+            const int f = I.cf_face[j];
+            const double sA = (I.fown[f] == c ? 1.0 : -1.0) * I.farea64[f];
+            const double *fs = I.fsum + (size_t)f * 4;
+            double F0, F1, F2, F3;
+            if (I.fbnd[f] >= 0) {
+                F0 = fs[0];
+                F1 = fs[1];
+                F2 = fs[2];
+                F3 = fs[3];
+            } else {
+                const double Cs = I.fmac[(size_t)f * 8 + 6], oCs = 1.0 - Cs;
+                const double *fb = I.fgbar + (size_t)f * 4;
+                F0 = oCs * fb[0] + Cs * fs[0];
+                F1 = oCs * fb[1] + Cs * fs[1];
+                F2 = oCs * fb[2] + Cs * fs[2];
+                F3 = oCs * fb[3] + Cs * fs[3];
+            }
+            m0 += sA * F0;
+            m1x += sA * F1;
+            m1y += sA * F2;
+            m2 += sA * F3;
+        }
+        I.fm0[c] = m0;
+        I.fm1[3 * c] = m1x;
+        I.fm1[3 * c + 1] = m1y;
+        I.fm1[3 * c + 2] = 0.0;
+        I.fm2[c] = m2;
+        // conservative update (cdugks_shakhov.cpp:645-660)
+        const double dt_v = I.dt / I.vol[c];
+        const double rho_n = I.rho[c], unx = I.u[3 * c], uny = I.u[3 * c + 1], T_n = I.T[c];
+        const double qnx = I.q[3 * c], qny = I.q[3 * c + 1];
+        const double rhoE_n = rho_n * (0.5 * (unx * unx + uny * uny) + I.Cv * T_n);
+        const double tau_n = tau_f(I, rho_n, T_n);
+        const double rho = rho_n - dt_v * m0;
+        const double rux = rho_n * unx - dt_v * m1x, ruy = rho_n * uny - dt_v * m1y;
+        const double rhoE = rhoE_n - dt_v * 0.5 * m2;
+        const double ux = rux / rho, uy = ruy / rho;
+        const double T = (rhoE / rho - 0.5 * (ux * ux + uy * uy)) / I.Cv;
+        const double tau = tau_f(I, rho, T);
+        I.rho[c] = rho;
+        I.u[3 * c] = ux;
+        I.u[3 * c + 1] = uy;
+        I.u[3 * c + 2] = 0.0;
+        I.T[c] = T;
+        I.u32[c] = make_float2((float)ux, (float)uy);
+        CellK k;
+        const double RTn = I.R * T_n, pn = rho_n * RTn, RT = I.R * T, p = rho * RT;
+        k.unx = (float)unx;
+        k.uny = (float)uny;
+        k.qnx = (float)qnx;
+        k.qny = (float)qny;
+        k.An = (float)(rho_n / (2.0 * kPI * RTn));
+        k.bln = (float)(kLOG2E / (2.0 * RTn));
+        k.sgn = (float)((1.0 - I.Pr) / (5.0 * pn * RTn));
+        k.shn = (float)((1.0 - I.Pr) / (5.0 * pn));
+        k.iRTn = (float)(1.0 / RTn);
+        k.hmn = (float)((I.Kd + 1.0) * RTn);
+        k.ux = (float)ux;
+        k.uy = (float)uy;
+        k.A = (float)(rho / (2.0 * kPI * RT));
+        k.bl = (float)(kLOG2E / (2.0 * RT));
+        k.sg = (float)((1.0 - I.Pr) / (5.0 * p * RT));
+        k.sh = (float)((1.0 - I.Pr) / (5.0 * p));
+        k.iRT = (float)(1.0 / RT);
+        k.hm = (float)((I.Kd + 1.0) * RT);
+        k.cm = (float)(I.hdt / (I.hdt - 2.0 * tau_n));
+        k.C = (float)(tau / (tau + I.hdt));
+        k.Cs = (float)(I.hdt / (2.0 * tau));
+        k.hdt_tau = (float)(I.hdt / tau);
+        k.hdt_taun = (float)(I.hdt / tau_n);
+        k.dt_v = (float)dt_v;
+        I.ck[c] = k;
+        // monitor (cdugks_shakhov.cpp:697-719)
+        if (isnan(rho) || T < 0.0 || isnan(T)) {
+            DStatus *st = I.status;
+            atomicAdd(&st->bad_count, 1);
+            atomicMin(&st->first_bad, c);
+            if (I.mask && I.mask[c]) {
+                int slot = atomicAdd(&st->repair_count, 1);
+                if (slot < I.C) I.repair_list[slot] = c;
+            } else {
+                atomicMin(&st->stop_step, st->step);
+            }
+        }
+    }
+}
+
+// =============================================================================
+// P2: face values, flux, evolution, heat-flux partials
+// =============================================================================
+__global__ void __launch_bounds__(kT, 2) k32_update(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
+                                                   int nitems, int cur) {
+    extern __shared__ float4 smem_raw[];
+    const Smem sm = smem_layout(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int2 item = items[it];
+        const F32Inst &I = insts[item.x];
+        if (step_stopped(I.status)) continue;
+        const int tile = item.y / I.ngroup, grp = item.y % I.ngroup;
+        const int cs = I.tile_cstart[tile], nc = I.tile_ncell[tile];
+        const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
+        const int ch0 = grp * cpg, ch1 = min(I.chunks, ch0 + cpg);
+        const float2 *S = I.S[cur];
+        float2 *Sn = I.S[cur ^ 1];
+        const float hdt = (float)I.hdt;
+        const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
+        const size_t NVp = (size_t)I.NVp;
+        for (int k = threadIdx.x; k < nc * 4; k += kT) sm.acc[k] = 0.f;
+        for (int ch = ch0; ch < ch1; ++ch) {
+            const int p = ch * 32 + lane;
+            stage_chunk(I, S, tile, p, sm);
+            const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
+            const float hx = hdt * xx, hy = hdt * xy;
+            for (int cl = warp; cl < nc; cl += F32_WARPS) {
+                const int c = cs + cl;
+                float fg = 0.f, fh = 0.f;
+                for (int j = I.cf_ptr[c]; j < I.cf_ptr[c + 1]; ++j) {
+                    const int f = I.cf_face[j];
+                    const bool own = I.fown[f] == c;
+                    const float2 n = I.fn32[f];
+                    const float d = fmaf(n.x, xx, n.y * xy);
+                    const float knA = (own ? d : -d) * I.farea[f];
+                    const int b = I.fbnd[f];
+                    float2 gf;
+                    if (b >= 0) {
+                        gf = I.bnd_out[(size_t)b * NVp + p];
+                    } else {
+                        const int o = I.cf_oslot[j];
+                        const int os = own ? cl : o, ns = own ? o : cl;
+                        const int cls = classify(I, f, p, d, xx, xy);
+                        const float2 gb = face_bar(I, sm, f, cls, os, ns, hx, hy);
+                        const FaceK k = I.fk[f];
+                        const float2 gs = shakhov(xx - k.ux, xy - k.uy, k.A, k.bl, k.qx, k.qy, k.sg, k.sh, k.iRT, k.hm,
+                                                  k3, twoK);
+                        gf = make_float2(fmaf(k.oCs, gb.x, k.Cs * gs.x), fmaf(k.oCs, gb.y, k.Cs * gs.y));
+                    }
+                    fg = fmaf(knA, gf.x, fg);
+                    fh = fmaf(knA, gf.y, fh);
+                }
+                const CellK k = I.ck[c];
+                const float2 old = sm.phi[cl * 32 + lane];
+                // state n (cdugks_shakhov.cpp:673-680)
+                const float2 sn = shakhov(xx - k.unx, xy - k.uny, k.An, k.bln, k.qnx, k.qny, k.sgn, k.shn, k.iRTn,
+                                          k.hmn, k3, twoK);
+                const float gn = fmaf(k.cm, sn.x - old.x, old.x);
+                const float hn = fmaf(k.cm, sn.y - old.y, old.y);
+                // state n+1 with q at n (:682-687)
+                const float cx = xx - k.ux, cy = xy - k.uy;
+                const float2 s1 = shakhov(cx, cy, k.A, k.bl, k.qnx, k.qny, k.sg, k.sh, k.iRT, k.hm, k3, twoK);
+                // evolution (:689-690)
+                const float g = k.C * (gn + k.hdt_tau * s1.x + k.hdt_taun * (sn.x - gn) - k.dt_v * fg);
+                const float h = k.C * (hn + k.hdt_tau * s1.y + k.hdt_taun * (sn.y - hn) - k.dt_v * fh);
+                // heat flux partial (:692) and f-bar-plus (:694-695)
+                const float hw = 0.5f * w * fmaf(fmaf(cx, cx, cy * cy), g, h);
+                float qv[2] = {hw * cx, hw * cy};
+                Sn[(size_t)c * NVp + p] = make_float2(fmaf(k.Cs, s1.x - g, g), fmaf(k.Cs, s1.y - h, h));
+                warp_sum(qv);
+                if (lane < 2) {
+                    float *a = sm.acc + cl * 4 + 2 * lane;
+                    kahan(a[0], a[1], lane == 0 ? qv[0] : qv[1]);
+                }
+            }
+            __syncthreads();
+        }
+        for (int k = threadIdx.x; k < nc * 2; k += kT) {
+            const int cl = k >> 1, comp = k & 1;
+            I.qpart[((size_t)grp * I.C + cs + cl) * 2 + comp] = (double)sm.acc[cl * 4 + 2 * comp] -
+                                                                  (double)sm.acc[cl * 4 + 2 * comp + 1];
+        }
+        __syncthreads();
+    }
+}
+
+// =============================================================================
+// QR: heat flux from the partials; mask repair; end of step
+// =============================================================================
+__global__ void k32_heat_flux(const F32Inst *__restrict__ insts, const int *__restrict__ coff, int ninst, int total,
+                              int count_step) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int i = find_inst(coff, ninst, g);
+        const F32Inst &I = insts[i];
+        if (count_step && step_stopped(I.status)) continue;
+        const int c = g - coff[i];
+        double qx = 0.0, qy = 0.0;
+        for (int grp = 0; grp < I.ngroup; ++grp) {
+            qx += I.qpart[((size_t)grp * I.C + c) * 2];
+            qy += I.qpart[((size_t)grp * I.C + c) * 2 + 1];
+        }
+        I.q[3 * c] = qx;
+        I.q[3 * c + 1] = qy;
+        I.q[3 * c + 2] = 0.0;
+    }
+}
+
+// cell_value_interp (cdugks_shakhov.cpp:766-789) for queued masked cells, writing state n+1
+__global__ void k32_mask_repair(const F32Inst *__restrict__ insts, int ninst, int nxt) {
+    for (int i = 0; i < ninst; ++i) {
+        const F32Inst &I = insts[i];
+        const int n = min(I.status->repair_count, I.C);
+        for (int r = blockIdx.x; r < n; r += gridDim.x) {
+            const int c = I.repair_list[r];
+            double sw = 0.0, sr = 0.0, sT = 0.0, sux = 0.0, suy = 0.0, sqx = 0.0, sqy = 0.0;
+            for (int j = I.cn_ptr[c]; j < I.cn_ptr[c + 1]; ++j) {
+                const double *dr = I.lsq_dr + 3 * (size_t)j;
+                const double wi = 1.0 / (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+                const int nb = I.cn_cell[j];
+                sw += wi;
+                sr += wi * I.rho[nb];
+                sT += wi * I.T[nb];
+                sux += wi * I.u[3 * nb];
+                suy += wi * I.u[3 * nb + 1];
+                sqx += wi * I.q[3 * nb];
+                sqy += wi * I.q[3 * nb + 1];
+            }
+            const double rho = sr / sw, T = sT / sw, ux = sux / sw, uy = suy / sw, qx = sqx / sw, qy = sqy / sw;
+            const double RT = I.R * T, p = rho * RT;
+            const float A = (float)(rho / (2.0 * kPI * RT)), bl = (float)(kLOG2E / (2.0 * RT));
+            const float sg = (float)((1.0 - I.Pr) / (5.0 * p * RT)), sh = (float)((1.0 - I.Pr) / (5.0 * p));
+            const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
+            for (int pp = threadIdx.x; pp < I.NVp; pp += blockDim.x)
+                I.S[nxt][(size_t)c * I.NVp + pp] =
+                    shakhov(I.xi32x[pp] - (float)ux, I.xi32y[pp] - (float)uy, A, bl, (float)qx, (float)qy, sg, sh,
+                            (float)(1.0 / RT), (float)((I.Kd + 1.0) * RT), k3, twoK);
+            if (threadIdx.x == 0) {
+                I.rho[c] = rho;
+                I.T[c] = T;
+                I.u[3 * c] = ux;
+                I.u[3 * c + 1] = uy;
+                I.u32[c] = make_float2((float)ux, (float)uy);
+            }
+        }
+    }
+}
+
+__global__ void k32_end_step(const F32Inst *__restrict__ insts, int ninst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    DStatus *st = insts[i].status;
+    if (st->stop_step < st->step) return;
+    st->repairs_total += st->repair_count;
+    st->repair_count = 0;
+    st->step += 1;
+}
+
+// =============================================================================
+// initial(): FP64 equilibrium per velocity, stored in FP32; FP64 moments
+// (cdugks_shakhov.cpp:81-168).  One warp per cell.
+// =============================================================================
+__global__ void k32_init(const F32Inst *__restrict__ insts, const int *__restrict__ coff, int ninst, int total,
+                         int mode, int cur) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
+        const int i = find_inst(coff, ninst, g);
+        const F32Inst &I = insts[i];
+        const int c = g - coff[i];
+        const double r = I.rho[c], ux = I.u[3 * c], uy = I.u[3 * c + 1], T = I.T[c];
+        const double qx = I.q[3 * c], qy = I.q[3 * c + 1];
+        const double RT = I.R * T, over = 0.5 / RT, p = r * RT;
+        double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int pp = lane; pp < I.NVp; pp += 32) {
+            const double xx = I.xi64x[pp], xy = I.xi64y[pp], w = I.w64[pp];
+            const double cx = xx - ux, cy = xy - uy, cc = cx * cx + cy * cy;
+            const double gm = r * over / kPI * exp(-cc * over);
+            double gg, hh;
+            if (mode == 0) {
+                gg = gm;
+                hh = (I.Kd + 1.0) * RT * gm;
+            } else {
+                const double cq = cx * qx + cy * qy;
+                gg = (1.0 - I.Pr) * (cq / (5.0 * p * RT)) * (cc / RT - 4.0) * gm + gm;
+                hh = (1.0 - I.Pr) * (cq / (5.0 * p)) * ((cc / RT - 2.0) * (I.Kd + 1.0) - 2.0 * I.Kd) * gm +
+                     (I.Kd + 1.0) * RT * gm;
+            }
+            I.S[cur][(size_t)c * I.NVp + pp] = make_float2((float)gg, (float)hh);
+            v[0] += w * gg;
+            v[1] += w * gg * xx;
+            v[2] += w * gg * xy;
+            v[3] += w * ((xx * xx + xy * xy) * gg + hh);
+            const double s = cc * gg + hh;
+            v[4] += w * cx * s;
+            v[5] += w * cy * s;
+        }
+        for (int k = 0; k < 6; ++k)
+            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+        if (lane == 0) {
+            if (mode == 0) {
+                const double rho = v[0], vx = v[1] / rho, vy = v[2] / rho;
+                I.rho[c] = rho;
+                I.u[3 * c] = vx;
+                I.u[3 * c + 1] = vy;
+                I.u[3 * c + 2] = 0.0;
+                I.T[c] = (0.5 * v[3] / rho - 0.5 * (vx * vx + vy * vy)) / I.Cv;
+                I.q[3 * c] = 0.5 * v[4];
+                I.q[3 * c + 1] = 0.5 * v[5];
+                I.q[3 * c + 2] = 0.0;
+            }
+            I.u32[c] = make_float2((float)I.u[3 * c], (float)I.u[3 * c + 1]);
+        }
+    }
+}
+
+int grid_of(int total, int per_block, int cap) {
+    int b = (total + per_block - 1) / per_block;
+    return b < 1 ? 1 : (b < cap ? b : cap);
+}
+
+}  // namespace
+
+int fp32_configure(int device) {
+    (void)device;
+    if (cudaFuncSetAttribute(k32_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) != cudaSuccess)
+        return -1;
+    if (cudaFuncSetAttribute(k32_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) != cudaSuccess)
+        return -1;
+    return 0;
+}
+
+const char *const kFp32Phases[] = {"k32_moments", "k32_face_macros", "k32_face_eqflux", "k32_boundary",
+                                   "k32_cell_macros", "k32_update", "k32_heat_flux+repair+end"};
+
+int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev) {
+    const int sms = s.num_sms;
+    const int cap = sms * 32;
+    const int tile_grid = s.nitems < sms * 2 ? s.nitems : sms * 2;
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecord(ev[k], stream);
+    };
+    mark(0);
+    k32_moments<<<tile_grid, kT, kSmemBytes, stream>>>(s.d_inst, s.d_items, s.nitems, s.cur);
+    mark(1);
+    k32_face_macros<<<grid_of(s.total_faces, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
+                                                                          s.total_faces);
+    mark(2);
+    k32_face_eqflux<<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
+                                                                        s.total_faces);
+    mark(3);
+    int n = 3;
+    if (s.total_bnd > 0) {
+        k32_boundary<<<grid_of(s.total_bnd, 1, cap), 256, 0, stream>>>(s.d_inst, s.d_bnd_items, s.ninst, s.total_bnd);
+        ++n;
+    }
+    mark(4);
+    k32_cell_macros<<<grid_of(s.total_cells, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_cell_items, s.ninst,
+                                                                          s.total_cells);
+    mark(5);
+    k32_update<<<tile_grid, kT, kSmemBytes, stream>>>(s.d_inst, s.d_items, s.nitems, s.cur);
+    mark(6);
+    k32_heat_flux<<<grid_of(s.total_cells, 256, cap), 256, 0, stream>>>(s.d_inst, s.d_cell_items, s.ninst,
+                                                                        s.total_cells, 1);
+    k32_mask_repair<<<32, 256, 0, stream>>>(s.d_inst, s.ninst, s.cur ^ 1);
+    k32_end_step<<<(s.ninst + 63) / 64, 64, 0, stream>>>(s.d_inst, s.ninst);
+    mark(7);
+    n += 6;
+    if (launches) *launches += n;
+    s.cur ^= 1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int fp32_init(const Fp32State &s, int mode, cudaStream_t stream) {
+    k32_init<<<grid_of(s.total_cells, 8, s.num_sms * 32), 256, 0, stream>>>(s.d_inst, s.d_cell_items, s.ninst,
+                                                                           s.total_cells, mode, s.cur);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int fp32_finalize_q(const Fp32State &s, cudaStream_t stream) {
+    (void)s;
+    (void)stream;
+    return 0;
+}
+
+}  // namespace meso

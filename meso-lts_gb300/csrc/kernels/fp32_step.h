@@ -1,4 +1,9 @@
 // Host-visible interface of the FP32-storage Shakhov step (fp32_step.cu).
+//
+// One solve is an F32Inst: device pointers to its tile plan, geometry,
+// velocity set and state.  The phase kernels take an array of instances and
+// a work list of (instance, tile, velocity group) items, so one launch
+// serves one solve or a whole batch of solves of different sizes.
 #pragma once
 
 #include <cstdint>
@@ -8,8 +13,97 @@
 
 namespace meso {
 
+// Kernel limits (the tile planner shrinks tiles until every tile fits).
+constexpr int F32_LANES = 32;       // velocities per chunk (one per lane)
+constexpr int F32_WARPS = 8;        // warps per CTA
+constexpr int F32_MAX_SLOTS = 160;  // tile + two-ring halo cells
+constexpr int F32_MAX_GSLOTS = 112; // tile + one-ring halo cells (gradients)
+constexpr int F32_MAX_OWNED = 144;  // faces owned by a tile
+constexpr int F32_MAX_CELLS = 64;   // cells per tile
+constexpr int F32_NMOM = 11;        // raw face moments about the reference velocity (2-D)
+
+// Face equilibrium scalars for FP32 evaluation of g_S, h_S at a face.
+struct FaceK {
+    float ux, uy, qx, qy;
+    float A;    // rho / (2 pi R T)
+    float bl;   // log2(e) / (2 R T)
+    float sg;   // (1 - Pr) / (5 p R T)
+    float sh;   // (1 - Pr) / (5 p)
+    float iRT;  // 1 / (R T)
+    float hm;   // (K + 3 - D) R T
+    float Cs, oCs;
+};
+
+// Per-cell evolution constants (states n and n+1).
+struct CellK {
+    float unx, uny, qnx, qny, An, bln, sgn, shn, iRTn, hmn;
+    float ux, uy, A, bl, sg, sh, iRT, hm;
+    float cm, C, Cs, hdt_tau, hdt_taun, dt_v;
+};
+
+struct F32Inst {
+    int C, F, NV, NVp, nb, ntile, ngroup, chunks;  // chunks = NVp / 32
+    // physics
+    double dt, hdt, R, Pr, mu0, vhs, T0, Kd, Cv, gamma;
+    int gradient;
+    // tile plan
+    const int *tile_cstart, *tile_ncell, *tile_slot_ptr, *slot_cell, *tile_gslots, *tile_gsp_off, *gs_ptr;
+    const uint16_t *gs_nbr;
+    const float *gs_ax, *gs_ay;
+    const int *tile_fstart;
+    const uint16_t *face_own_slot, *face_nei_slot, *cf_oslot;
+    // mesh (renumbered)
+    const int *cf_ptr, *cf_face, *fown, *fnei, *fbnd, *bface, *fmark;
+    const float2 *fn32, *fdo, *fdn;
+    const double2 *fn64;
+    const float *farea;
+    const double *vol, *farea64, *fn64raw;
+    const meso_mark_desc *marks;
+    const uint8_t *mask;
+    const int *cn_ptr, *cn_cell;
+    const double *lsq_dr;
+    // velocities (padded to NVp with zero weight)
+    const float *xi32x, *xi32y, *w32;
+    const double *xi64x, *xi64y, *w64;
+    const int *sym;
+    // state and work buffers
+    float2 *S[2];          // [C][NVp] (g, h) ping-pong
+    double *fpart;         // [ngroup][F][11] raw face-moment partials
+    float2 *u32;           // [C] cell velocity (FP32) = reference velocity of the face moments
+    FaceK *fk;             // [F]
+    double *fmac;          // [F][8] rho, ux, uy, T, qx, qy, Cs, tau
+    double *fgbar;         // [F][4] fluxes of the reconstructed values (mass, mom x, mom y, energy) per unit area along n0
+    double *fsum;          // [F][4] same for the face equilibrium (interior) or the final boundary values
+    float2 *bnd_in, *bnd_out;  // [nb][NVp]
+    CellK *ck;             // [C]
+    double *qpart;         // [ngroup][C][2]
+    double *rho, *u, *T, *q;   // [C], [3C], [C], [3C]
+    double *fm0, *fm1, *fm2;   // flux moments
+    int *repair_list;
+    DStatus *status;
+};
+
+// Host-side handle of one or more instances sharing the phase launches.
 struct Fp32State {
     int enabled = 0;
+    int ninst = 0;
+    F32Inst *d_inst = nullptr;   // device copy of the instance array
+    int2 *d_items = nullptr;     // (inst, tile * ngroup + group) work items
+    int nitems = 0;
+    int *d_face_items = nullptr; // prefix sums of faces / cells / boundary faces over instances
+    int *d_cell_items = nullptr;
+    int *d_bnd_items = nullptr;
+    int total_faces = 0, total_cells = 0, total_bnd = 0;
+    int num_sms = 0;
+    int cur = 0;                 // which S buffer holds the current state
 };
+
+int fp32_configure(int device);
+constexpr int F32_NPHASE = 7;
+extern const char *const kFp32Phases[F32_NPHASE];
+// One step of every instance; ev (may be null) receives F32_NPHASE + 1 events around the phases.
+int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev = nullptr);
+int fp32_init(const Fp32State &s, int mode, cudaStream_t stream);
+int fp32_finalize_q(const Fp32State &s, cudaStream_t stream);
 
 }  // namespace meso

@@ -889,7 +889,10 @@ int grid_for(size_t total, int sms) {
 }
 
 template <int DIM>
-int plain_step_dim(const PlainState &s, cudaStream_t stream, int64_t *launches) {
+int plain_step_dim(const PlainState &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev) {
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecord(ev[k], stream);
+    };
     const DMesh &m = s.mesh;
     const KParams &k = s.kp;
     const int L = seg_lanes(m.NV);
@@ -897,20 +900,25 @@ int plain_step_dim(const PlainState &s, cudaStream_t stream, int64_t *launches) 
     const int sms = s.num_sms;
     const size_t cv = (size_t)m.C * m.NV, fv = (size_t)m.F * m.NV;
     int64_t n = 0;
+    mark(0);
     if (s.solver == MESO_SOLVER_CDUGKS_SHAKHOV) {
         if (k.gradient) {
             k_grad<DIM, 2><<<grid_for(cv, sms), kBlock, 0, stream>>>(m, s.status, s.f0, s.f1, s.grad0, s.grad1);
             ++n;
         }
+        mark(1);
         k_recon<DIM, 2, true><<<grid_for(fv, sms), kBlock, 0, stream>>>(m, k, s.status, s.f0, s.f1, s.grad0, s.grad1,
                                                                          s.face0, s.face1);
+        mark(2);
         k_face_eq<DIM, true><<<(m.F + spb - 1) / spb, kBlock, 0, stream>>>(m, k, s.status, L, s.face0, s.face1);
+        mark(3);
         n += 2;
         if (m.nb > 0) {
             k_boundary<DIM, true><<<m.nb, L, 0, stream>>>(m, k, s.status, s.rho, s.u, s.T, s.face0, s.face1, s.snap0,
                                                           s.snap1);
             ++n;
         }
+        mark(4);
         k_update_shakhov<DIM><<<(m.C + spb - 1) / spb, kBlock, 0, stream>>>(
             m, k, s.status, L, s.f0, s.f1, s.face0, s.face1, s.flux0, s.flux1, s.rho, s.u, s.T, s.q, s.fm0, s.fm1,
             s.fm2, s.repair_list);
@@ -921,15 +929,19 @@ int plain_step_dim(const PlainState &s, cudaStream_t stream, int64_t *launches) 
             k_grad<DIM, 1><<<grid_for(cv, sms), kBlock, 0, stream>>>(m, s.status, s.f0, nullptr, s.grad0, nullptr);
             ++n;
         }
+        mark(1);
         k_recon<DIM, 1, false><<<grid_for(fv, sms), kBlock, 0, stream>>>(m, k, s.status, s.f0, nullptr, s.grad0,
                                                                           nullptr, s.face0, nullptr);
+        mark(2);
         k_face_eq<DIM, false><<<(m.F + spb - 1) / spb, kBlock, 0, stream>>>(m, k, s.status, L, s.face0, nullptr);
+        mark(3);
         n += 2;
         if (m.nb > 0) {
             k_boundary<DIM, false><<<m.nb, L, 0, stream>>>(m, k, s.status, s.rho, s.u, s.T, s.face0, nullptr, s.snap0,
                                                            nullptr);
             ++n;
         }
+        mark(4);
         if (s.solver == MESO_SOLVER_CDUGKS)
             k_update_cdugks<DIM><<<(m.C + spb - 1) / spb, kBlock, 0, stream>>>(m, k, s.status, L, s.f0, s.face0,
                                                                                s.flux0, s.rho, s.u);
@@ -938,7 +950,9 @@ int plain_step_dim(const PlainState &s, cudaStream_t stream, int64_t *launches) 
                                                                               s.u);
         ++n;
     }
+    mark(5);
     k_end_step<<<1, 32, 0, stream>>>(s.status);
+    mark(6);
     ++n;
     if (launches) *launches += n;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
@@ -964,8 +978,10 @@ int plain_init_dim(const PlainState &s, int mode, cudaStream_t stream) {
 
 }  // namespace
 
-int plain_step(const PlainState &s, cudaStream_t stream, int64_t *launches) {
-    return s.mesh.dim == 2 ? plain_step_dim<2>(s, stream, launches) : plain_step_dim<3>(s, stream, launches);
+const char *const kPlainPhases[] = {"k_grad", "k_recon", "k_face_eq", "k_boundary", "k_update+repair", "k_end_step"};
+
+int plain_step(const PlainState &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev) {
+    return s.mesh.dim == 2 ? plain_step_dim<2>(s, stream, launches, ev) : plain_step_dim<3>(s, stream, launches, ev);
 }
 
 int plain_init(const PlainState &s, int mode, cudaStream_t stream) {

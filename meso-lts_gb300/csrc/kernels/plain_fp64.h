@@ -25,7 +25,10 @@ struct PlainState {
     int *repair_list;         // [C]
 };
 
-int plain_step(const PlainState &s, cudaStream_t stream, int64_t *launches);
+constexpr int PLAIN_NPHASE = 6;
+extern const char *const kPlainPhases[PLAIN_NPHASE];
+// One step; ev (may be null) receives PLAIN_NPHASE + 1 events around the phases.
+int plain_step(const PlainState &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev = nullptr);
 int plain_init(const PlainState &s, int mode, cudaStream_t stream);
 
 }  // namespace meso

@@ -102,6 +102,8 @@ _SIGS = {
     "meso_ctx_device_bytes": (C.c_size_t, [C.c_void_p]),
     "meso_last_step_ms": (C.c_double, [C.c_void_p]),
     "meso_last_step_launches": (C.c_int64, [C.c_void_p]),
+    "meso_phase_times": (C.c_int, [C.c_void_p, C.c_int32, _dp, C.c_int32, _ip]),
+    "meso_phase_name": (C.c_char_p, [C.c_void_p, C.c_int32]),
 }
 
 EXPORTED = tuple(_SIGS)
@@ -294,6 +296,13 @@ class Solver:
 
     def last_step_launches(self) -> int:
         return lib().meso_last_step_launches(self._h)
+
+    def phase_times(self, nsteps: int) -> dict:
+        """Mean device ms per step of each kernel phase over nsteps real steps."""
+        ms = np.zeros(16)
+        n = C.c_int32()
+        _check(lib().meso_phase_times(self._h, nsteps, _ptr(ms), 16, C.byref(n)))
+        return {lib().meso_phase_name(self._h, i).decode(): float(ms[i]) for i in range(n.value)}
 
     @property
     def handle(self):

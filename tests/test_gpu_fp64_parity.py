@@ -21,6 +21,7 @@ from conftest import GOLDEN
 from helpers import max_field_err, relerr, run_gpu, run_oracle
 
 TOL = 1e-12
+THRESHOLD_SENSITIVE = {"shakhov_q8_limiter"}
 GOLDEN_NAMES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("geometry_"))
 
 
@@ -44,8 +45,16 @@ def test_fp64_matches_reference_outputs(gpu, name):
         s.close()
         return
     assert r["step"] == int(g["step"])
+    tol = dict.fromkeys(("rho", "u", "T", "q"), TOL)
+    if name in THRESHOLD_SENSITIVE:
+        # The Venkatakrishnan limiter returns 1 when |dw| <= eps (limiter.cpp:11), a jump that turns
+        # 1e-16 summation-order differences into O(1e-5) field differences.  The reference run on two
+        # velocity slices (its 2-rank MPI path) already differs from its 1-rank run by that much; the
+        # GPU must stay inside 4x that envelope.
+        o2 = run_oracle(path, steps, nthreads=2)
+        tol = {k: max(TOL, 4.0 * relerr(o2[k], g[k])) for k in tol}
     for k in ("rho", "u", "T", "q"):
-        assert relerr(r[k], g[k]) <= TOL, (k, relerr(r[k], g[k]))
+        assert relerr(r[k], g[k]) <= tol[k], (k, relerr(r[k], g[k]), tol[k])
 
 
 CASES = [
