@@ -1,0 +1,379 @@
+#!/usr/bin/env python3
+"""Benchmark of the Shakhov CDUGKS step on one GB300 (or N replicas).
+
+Workload (the configuration the headline metric is quoted on): rarefied 2-D
+lid-driven cavity, Shakhov CDUGKS, 7690-cell unstructured mesh (Delaunay
+triangles inside a one-cell quad wall layer), Newton-Cotes 101x101 velocity
+set on [-5,5]^2 (10201 velocities), Kn = 1, Pr = 2/3, lid 0.15, diffuse walls,
+FP32 storage.  Synthetic inputs written by meso-lts_gb300/cases.py in the
+reference's own formats.
+
+Metric: cell-velocity updates per second (cells x velocities x steps / time).
+  value        device time of K steps (CUDA events on the library's stream),
+               state resident in HBM (1.3 GB, larger than L2)
+  e2e          the same through the C ABI with pinned host buffers: initial
+               fields copied host->device, K steps, the macroscopic fields read
+               back device->host after every step
+  fp64_*       the plain FP64 step on the same workload, and the FP32 form's
+               error against it after the same number of steps
+  roofline     the dominant kernel (k32_update): algorithmic bytes (16 B per
+               cell-velocity: g, h read and written in FP32) / its event-timed
+               duration, against the measured HBM copy bandwidth
+  cpu_baseline the oracle (CPU restatement of the reference step) on all host
+               cores, on a bounded sample of the same workload
+
+--impl reference times that CPU implementation alone (rank 0) on the same
+workload and prints the same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in ("meso-lts_gb300", "oracle"):
+    sys.path.insert(0, os.path.join(ROOT, _p))
+
+import numpy as np  # noqa: E402
+
+METRIC = "cell-xi updates/s (FP32-storage Shakhov CDUGKS step)"
+UNIT = "cell-xi/s"
+WORKLOAD = ("rarefied 2-D cavity, Shakhov CDUGKS, 7690-cell unstructured mesh (Delaunay triangles in a quad wall "
+            "layer), Newton-Cotes 101x101 DVS on [-5,5]^2, Kn=1, Pr=2/3, lid 0.15, FP32 storage")
+
+
+def _cudart():
+    for name in ("libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            continue
+    raise RuntimeError("libcudart not found")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Host-side barrier and max over ranks (the replicas exchange no data)."""
+
+    def __init__(self, world: int):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic() -> float | None:
+    """DRAM bytes per k32_update launch from the committed ncu summary (profiles/), if present."""
+    p = os.path.join(ROOT, "profiles", "k32_update_config2.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["dram_bytes_per_launch"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def build_workload(tmp: str, precision: str) -> str:
+    import cases
+
+    return cases.config2(os.path.join(tmp, f"config2_{precision}"), steps=500, precision=precision)
+
+
+def relerr(a, b) -> float:
+    s = float(np.max(np.abs(b)))
+    return float(np.max(np.abs(a - b))) / s if s > 0 else float(np.max(np.abs(a)))
+
+
+def pinned(n: int):
+    """numpy view of page-locked host memory (cudaHostAlloc)."""
+    rt = _cudart()
+    p = ctypes.c_void_p()
+    if rt.cudaHostAlloc(ctypes.byref(p), ctypes.c_size_t(n * 8), 0) != 0:
+        return np.zeros(n)
+    buf = (ctypes.c_double * n).from_address(p.value)
+    return np.frombuffer(buf, dtype=np.float64)
+
+
+def cpu_baseline(path: str, steps: int, threads: int) -> dict:
+    import meso_gpu as mg
+    import meso_oracle as mo
+
+    case = mg.Case(path)
+    rho, u, T, mask = case.initial_fields()
+    o = mo.Oracle(case, threads, mask)
+    o.init(rho, u, T, None, 0)
+    t0 = time.perf_counter()
+    done, _ = o.step(steps)
+    secs = time.perf_counter() - t0
+    o.close()
+    cx = case.ncell * case.nv
+    return {"value": cx * done / secs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{done} full step(s) of the workload ({case.ncell} cells x {case.nv} velocities) on "
+                      f"{threads} threads, velocity set split as the reference's MPI ranks split it",
+            "seconds": secs}
+
+
+def run_reference(args, rank: int, dist: Dist) -> None:
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as tmp:
+        path = build_workload(tmp, "fp64")
+        threads = os.cpu_count() or 1
+        steps = max(1, min(args.steps, 3))
+        warm = 1 if args.warmup > 0 else 0
+        import meso_gpu as mg
+        import meso_oracle as mo
+
+        case = mg.Case(path)
+        rho, u, T, mask = case.initial_fields()
+        o = mo.Oracle(case, threads, mask)
+        o.init(rho, u, T, None, 0)
+        if warm:
+            o.step(warm)
+        t0 = time.perf_counter()
+        done, _ = o.step(steps)
+        secs = time.perf_counter() - t0
+        cx = case.ncell * case.nv
+        v = cx * done / secs
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": done, "warmup": warm, "ms_per_step": secs * 1e3 / done, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "cells": case.ncell, "velocities": case.nv},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"{done} of the requested {args.steps} steps (bounded), "
+                                           f"{warm} warm-up step(s), {threads} threads"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    dist = Dist(world)
+    if args.impl == "reference":
+        run_reference(args, rank, dist)
+        dist.close()
+        return 0
+
+    rt = _cudart()
+    rt.cudaSetDevice(local)
+    import meso_gpu as mg
+
+    with tempfile.TemporaryDirectory() as tmp:
+        path = build_workload(tmp, "fp32")
+        case = mg.Case(path)
+        rho, u, T, mask = case.initial_fields()
+        C, NV = case.ncell, case.nv
+        cx = C * NV
+        K, W = args.steps, args.warmup
+
+        # ---- device-timed FP32 step, state resident
+        s = mg.Solver(case=case, precision=mg.FP32, mask=mask)
+        s.init_macros(rho, u, T, None, 0)
+        s.step(W)
+        dist.barrier()
+        rt.cudaDeviceSynchronize()
+        with ClockSampler(local) as clk:
+            done = s.step(K)
+            rt.cudaDeviceSynchronize()
+        ms = s.last_step_ms()
+        launches = s.last_step_launches()
+        st = s.status()
+        ok = done == K and st.run_state == 1
+        ms_max = dist.max(ms)
+        total_cx = dist.sum(float(cx * K))
+        value = total_cx / (ms_max * 1e-3)
+        # phase times (events on the library's stream) for the roofline of the dominant kernel
+        phases = s.phase_times(5)
+        fp32_macros = None
+        s.close()
+
+        # ---- plain FP64 step on the same workload (fewer steps: it is ~8x slower)
+        K64 = max(3, K // 10)
+        s64 = mg.Solver(case=case, precision=mg.FP64, mask=mask)
+        s64.init_macros(rho, u, T, None, 0)
+        s64.step(1)
+        s64.step(K64)
+        ms64 = s64.last_step_ms()
+        fp64_value = cx * K64 / (ms64 * 1e-3)
+        # error of the FP32 form against FP64 after the same number of steps
+        nerr = 1 + K64
+        b = s64.macros(C)
+        s64.close()
+        s32 = mg.Solver(case=case, precision=mg.FP32, mask=mask)
+        s32.init_macros(rho, u, T, None, 0)
+        s32.step(nerr)
+        a = s32.macros(C)
+        s32.close()
+        err = {k: relerr(x, y) for k, x, y in zip(("rho", "u", "T", "q"), a, b)}
+
+        # ---- e2e through the C ABI with pinned host buffers
+        hr, hu, hT = pinned(C), pinned(3 * C), pinned(C)
+        hr[:] = rho
+        hu[:] = u.reshape(-1)
+        hT[:] = T
+        orho, ou, oT, oq = pinned(C), pinned(3 * C), pinned(C), pinned(3 * C)
+        e = mg.Solver(case=case, precision=mg.FP32, mask=mask)
+        L = mg.lib()
+        P = lambda x: x.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        L.meso_init_macros(e.handle, P(hr), P(hu), P(hT), None, 0)
+        e.step(W)
+        dist.barrier()
+        rt.cudaDeviceSynchronize()
+        t0 = time.perf_counter()
+        L.meso_init_macros(e.handle, P(hr), P(hu), P(hT), None, 0)
+        for _ in range(K):
+            e.step(1)
+            L.meso_get_macros(e.handle, P(orho), P(ou), P(oT), P(oq))
+        rt.cudaDeviceSynchronize()
+        e2e_secs = dist.max(time.perf_counter() - t0)
+        e.close()
+        e2e_value = total_cx / e2e_secs
+        h2d = (C + 3 * C + C) * 8 / K
+        d2h = (C + 3 * C + C + 3 * C) * 8
+
+        peak, peak_kind = measured_peak_hbm()
+        upd_ms = phases.get("k32_update", None)
+        alg_bytes = 16.0 * cx
+        achieved = alg_bytes / (upd_ms * 1e-3) / 1e9 if upd_ms else None
+        traffic = ncu_traffic()
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (FP64 moments and equilibria)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": C, "velocities": NV, "state_bytes": 16 * cx,
+                       "l2": "state (1.3 GB, two buffers) larger than L2; no flush needed",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "run_ok": ok,
+            "fp64_value": fp64_value, "fp64_ms_per_step": ms64 / K64, "fp32_over_fp64": value / world / fp64_value,
+            "fp32_error_vs_fp64": {"steps": nerr, **err},
+            "phases_ms": phases,
+            "roofline": {"bound": "hbm", "kernel": "k32_update", "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak if achieved else None,
+                         "traffic": traffic, "alg_bytes_per_launch": alg_bytes},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "note": "initial fields host->device once per K steps; macros device->host every step"},
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+        }
+        if rank == 0 and world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(path, 1, os.cpu_count() or 1)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -110,6 +110,45 @@ def quad_channel(path: str, nx: int, ny: int, lx: float = 2.0, ly: float = 1.0) 
     return dict(ncell=nx * ny, min_cell_size=2.0 * math.sqrt(hx * hy / math.pi))
 
 
+def jquad_cavity(path: str, n: int, seed: int = 0, jitter: float = 0.25) -> dict:
+    """n x n unstructured quadrilaterals: lattice nodes moved by up to `jitter` h (wall nodes slide along
+    their wall, corners fixed), seeded; every cell is a convex quad with an over-determined gradient."""
+    rng = np.random.default_rng(seed)
+    h = 1.0 / n
+    P = np.zeros((n + 1, n + 1, 2))
+    for j in range(n + 1):
+        for i in range(n + 1):
+            x, y = i * h, j * h
+            if 0 < i < n:
+                x += rng.uniform(-jitter, jitter) * h
+            if 0 < j < n:
+                y += rng.uniform(-jitter, jitter) * h
+            P[j, i] = (x if i < n else 1.0, y if j < n else 1.0)
+    nodes = P.reshape(-1, 2)
+    nid = lambda i, j: j * (n + 1) + i
+    cells, lid, wall = [], [], []
+    amin = 1e300
+    for j in range(n):
+        for i in range(n):
+            c = len(cells)
+            q = [nid(i, j), nid(i + 1, j), nid(i + 1, j + 1), nid(i, j + 1)]
+            cells.append(q)
+            a1, a2 = _tri_area(nodes, [q[0], q[1], q[2]]), _tri_area(nodes, [q[0], q[2], q[3]])
+            b1, b2 = _tri_area(nodes, [q[0], q[1], q[3]]), _tri_area(nodes, [q[1], q[2], q[3]])
+            assert min(a1, a2, b1, b2) > 0, "non-convex quad"
+            amin = min(amin, a1 + a2)
+            if j == n - 1:
+                lid.append((c, 2, 3))
+            if j == 0:
+                wall.append((c, 2, 1))
+            if i == n - 1:
+                wall.append((c, 2, 2))
+            if i == 0:
+                wall.append((c, 2, 4))
+    _write_neu(path, nodes, cells, 2, {"lid": lid, "wall": wall})
+    return dict(ncell=n * n, min_cell_size=2.0 * math.sqrt(amin / math.pi))
+
+
 def _tri_area(p, t):
     a, b, c = p[t[0]], p[t[1]], p[t[2]]
     return 0.5 * ((b[0] - a[0]) * (c[1] - a[1]) - (b[1] - a[1]) * (c[0] - a[0]))
@@ -405,6 +444,8 @@ def shakhov_cavity(d: str, mesh: str = "quad", n: int = 61, dvs: str = "hgh", nv
     meshf = os.path.join(d, "mesh.neu")
     if mesh == "quad":
         info = quad_cavity(meshf, n)
+    elif mesh == "jquad":
+        info = jquad_cavity(meshf, n, seed)
     elif mesh == "mixed":
         info = mixed_cavity(meshf, n, seed)
     else:

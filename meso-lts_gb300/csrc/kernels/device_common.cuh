@@ -58,7 +58,8 @@ struct DStatus {
     int first_bad;      // smallest renumbered id of a bad cell
     int repair_count;   // masked cells queued for repair this step
     int repairs_total;
-    int pad[2];
+    int timeout;        // a bounded device wait gave up (the step's results are invalid)
+    int pad;
 };
 
 __device__ __forceinline__ bool step_stopped(const DStatus *st) { return st->stop_step < st->step; }
