@@ -2,10 +2,9 @@
 """Benchmark of the Shakhov CDUGKS step on one GB300 (or N replicas).
 
 Workload (the configuration the headline metric is quoted on): rarefied 2-D
-lid-driven cavity, Shakhov CDUGKS, 7690-cell unstructured mesh (Delaunay
-triangles inside a one-cell quad wall layer), Newton-Cotes 101x101 velocity
-set on [-5,5]^2 (10201 velocities), Kn = 1, Pr = 2/3, lid 0.15, diffuse walls,
-FP32 storage.  Synthetic inputs written by meso-lts_gb300/cases.py in the
+lid-driven cavity, Shakhov CDUGKS, 7744-cell unstructured mesh (seeded
+jittered quadrilaterals), Newton-Cotes 101x101 velocity set on [-5,5]^2
+(10201 velocities), Kn = 1, Pr = 2/3, lid 0.15, diffuse walls, FP32 storage.  Synthetic inputs written by meso-lts_gb300/cases.py in the
 reference's own formats.
 
 Metric: cell-velocity updates per second (cells x velocities x steps / time).
@@ -46,8 +45,8 @@ import numpy as np  # noqa: E402
 
 METRIC = "cell-xi updates/s (FP32-storage Shakhov CDUGKS step)"
 UNIT = "cell-xi/s"
-WORKLOAD = ("rarefied 2-D cavity, Shakhov CDUGKS, 7690-cell unstructured mesh (Delaunay triangles in a quad wall "
-            "layer), Newton-Cotes 101x101 DVS on [-5,5]^2, Kn=1, Pr=2/3, lid 0.15, FP32 storage")
+WORKLOAD = ("rarefied 2-D cavity, Shakhov CDUGKS, 7744-cell unstructured mesh (seeded jittered quadrilaterals), "
+            "Newton-Cotes 101x101 DVS on [-5,5]^2, Kn=1, Pr=2/3, lid 0.15, FP32 storage")
 
 
 def _cudart():

@@ -487,10 +487,12 @@ def config1(d: str, steps: int = 2000) -> str:
     return bgk_cavity(d, 64, steps)
 
 
-def config2(d: str, steps: int = 500, precision: str = "fp32", n: int = 64, nv1d: int = 101) -> str:
-    """Rarefied Shakhov cavity: 7686 unstructured cells (7434 Delaunay triangles inside a quad wall layer),
-    Newton-Cotes 101x101 on [-5,5]^2, Kn 1, lid 0.15."""
-    return shakhov_cavity(d, "mixed", n, "nc", nv1d, 1.0, 0.15, steps, seed=0, name="config2", precision=precision)
+def config2(d: str, steps: int = 500, precision: str = "fp32", n: int = 88, nv1d: int = 101) -> str:
+    """Rarefied Shakhov cavity: 7744 unstructured (jittered) quadrilaterals, Newton-Cotes 101x101 on [-5,5]^2,
+    Kn 1, lid 0.15.  (On Delaunay-triangle meshes of this size the reference scheme, whose least-squares
+    reconstruction is unlimited, grows an unstable mode before 500 steps; jittered quads keep the
+    unstructured geometry with over-determined gradients.)"""
+    return shakhov_cavity(d, "jquad", n, "nc", nv1d, 1.0, 0.15, steps, seed=0, name="config2", precision=precision)
 
 
 def config3(d: str, steps: int = 5000, precision: str = "fp32") -> str:

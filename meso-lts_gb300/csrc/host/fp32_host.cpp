@@ -14,15 +14,16 @@ bool plan_fp32(const meso_mesh_desc &m, int tile_cells, Renumbering &rn, TilePla
         std::vector<int> sizes;
         rn = renumber_tiled(m, T, sizes);
         if (build_tile_plan(m, rn, sizes, meso::F32_MAX_SLOTS, meso::F32_MAX_GSLOTS, meso::F32_MAX_OWNED,
-                            meso::F32_MAX_CELLS, plan))
+                            meso::F32_MAX_CELLS, plan) &&
+            plan.max_gentries <= meso::F32_MAX_GENT && plan.max_cf <= meso::F32_MAX_CF)
             return true;
     }
     return false;
 }
 
 int default_ngroup(int ntile, int chunks, int num_sms) {
-    // enough (tile, group) items for ~4 resident CTAs per SM, groups of at least 2 chunks
-    int want = (4 * num_sms + ntile - 1) / std::max(ntile, 1);
+    // ~6 (tile, group) items per persistent CTA (one per SM), groups of at least 2 chunks
+    int want = (6 * num_sms + ntile - 1) / std::max(ntile, 1);
     want = std::max(1, std::min(want, std::max(1, chunks / 2)));
     return want;
 }

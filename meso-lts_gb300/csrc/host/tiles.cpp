@@ -194,6 +194,7 @@ bool build_tile_plan(const meso_mesh_desc &m, const Renumbering &rn, const std::
             }
         }
         P.gs_ptr.push_back((int)P.gs_nbr.size());
+        P.max_gentries = std::max(P.max_gentries, P.gs_ptr.back() - P.gs_ptr[P.tile_gsp_off.back()]);
         // owned faces
         P.tile_fstart[t] = fcur;
         while (fcur < F && fown[fcur] < cs + n) {
@@ -202,6 +203,7 @@ bool build_tile_plan(const meso_mesh_desc &m, const Renumbering &rn, const std::
             ++fcur;
         }
         // per cell-face: slot of the cell on the other side
+        const size_t cf0 = P.cf_oslot.size();
         for (int c = cs; c < cs + n; ++c) {
             int o = rn.cell_new2old[c];
             for (int j = m.cell_face_ptr[o]; j < m.cell_face_ptr[o + 1]; ++j) {
@@ -210,6 +212,7 @@ bool build_tile_plan(const meso_mesh_desc &m, const Renumbering &rn, const std::
                 P.cf_oslot.push_back((uint16_t)slot_of[other]);
             }
         }
+        P.max_cf = std::max(P.max_cf, (int)(P.cf_oslot.size() - cf0));
         P.max_cells = std::max(P.max_cells, n);
         P.max_slots = std::max(P.max_slots, (int)slots.size());
         P.max_gslots = std::max(P.max_gslots, ng);

@@ -17,7 +17,7 @@
 namespace meso_host {
 
 struct TilePlan {
-    int ntile = 0, max_cells = 0, max_slots = 0, max_gslots = 0, max_owned = 0;
+    int ntile = 0, max_cells = 0, max_slots = 0, max_gslots = 0, max_owned = 0, max_gentries = 0, max_cf = 0;
     std::vector<int> tile_cstart, tile_ncell;        // [ntile]
     std::vector<int> tile_slot_ptr, slot_cell;       // slots: tile cells, 1-ring halo, 2-ring halo
     std::vector<int> tile_gslots;                    // [ntile] slots with a gradient (tile + 1-ring)

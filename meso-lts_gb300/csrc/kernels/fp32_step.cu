@@ -45,8 +45,6 @@ namespace {
 
 constexpr int kT = F32_WARPS * 32;
 constexpr double kLOG2E = 1.4426950408889634;
-constexpr size_t kSmemBytes =
-    sizeof(float2) * F32_MAX_SLOTS * 32 + sizeof(float4) * F32_MAX_GSLOTS * 32 + sizeof(float) * F32_MAX_OWNED * 24;
 
 __device__ __forceinline__ float fast_ex2(float x) {
     float y;
@@ -108,78 +106,216 @@ __device__ __forceinline__ int find_inst(const int *off, int n, int g) {
     return lo;
 }
 
-struct Smem {
-    float2 *phi;  // [F32_MAX_SLOTS][32]
-    float4 *G;    // [F32_MAX_GSLOTS][32]
-    float *acc;   // compensated accumulators (per owned face or per cell)
-};
-
-__device__ __forceinline__ Smem smem_layout(float4 *base) {
-    Smem s;
-    s.phi = reinterpret_cast<float2 *>(base);
-    s.G = reinterpret_cast<float4 *>(s.phi + F32_MAX_SLOTS * 32);
-    s.acc = reinterpret_cast<float *>(s.G + F32_MAX_GSLOTS * 32);
-    return s;
+// ---- TMA bulk copies and mbarriers (PTX ISA 8.0+, sm_90 and later) --------
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// One 256-byte velocity-contiguous segment (32 float2) from global to shared, completing on `bar`.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// Bounded wait: each try_wait suspends up to a hardware time limit; 2^22 tries is far beyond any copy.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+    for (int i = 0; i < (1 << 22); ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
 }
 
-// Stage the tile's slots for one chunk and compute the gradients of the first nG slots.
-__device__ __forceinline__ void stage_chunk(const F32Inst &I, const float2 *__restrict__ S, int tile, int p,
-                                            const Smem &sm) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+struct OwnedFace {     // P1: one face owned by the tile
+    float2 n, fdo, fdn, u0;
+    int bnd, face;
+    unsigned short os, ns;
+    int pad;
+};
+struct CellFace {      // P2: one face of a tile cell, seen from that cell
+    FaceK fk;
+    float2 n, fdo, fdn;
+    float area_s;      // +area if the cell owns the face, -area otherwise
+    int bnd, face;
+    unsigned short oslot;
+    unsigned char own, pad;
+};
+
+struct __align__(128) TileSmem {
+    float2 phi[2][F32_MAX_SLOTS * 32];  // double-buffered chunk of the tile + halo (TMA destination)
+    float4 G[F32_MAX_GSLOTS * 32];      // gradients (g_x, g_y, h_x, h_y) of tile + 1-ring cells
+    float2 ga[F32_MAX_GENT];            // gradient stencil coefficients
+    int slot_cell[F32_MAX_SLOTS];
+    unsigned short gnbr[F32_MAX_GENT];
+    unsigned short gptr[F32_MAX_GSLOTS + 1];
+    unsigned long long mbar[2];
+    int nS, nG, nX, base;
+    union {
+        struct {
+            OwnedFace of[F32_MAX_OWNED];
+            float acc[F32_MAX_OWNED * 22];
+        } p1;
+        struct {
+            CellK ck[F32_MAX_CELLS];
+            CellFace cf[F32_MAX_CF];
+            int cf_off[F32_MAX_CELLS + 1];
+            float acc[F32_MAX_CELLS * 4];
+        } p2;
+    } u;
+};
+
+constexpr size_t kTileSmem = sizeof(TileSmem);
+
+// Common per-item staging of the slot list and the gradient stencil.
+__device__ __forceinline__ void stage_common(const F32Inst &I, int tile, TileSmem &sm) {
     const int sbase = I.tile_slot_ptr[tile];
     const int nS = I.tile_slot_ptr[tile + 1] - sbase;
     const int nG = I.tile_gslots[tile];
-    const size_t NVp = (size_t)I.NVp;
-    for (int s = warp; s < nS; s += F32_WARPS) sm.phi[s * 32 + lane] = __ldg(S + (size_t)I.slot_cell[sbase + s] * NVp + p);
-    __syncthreads();
-    if (I.gradient) {
-        const int *gp = I.gs_ptr + I.tile_gsp_off[tile];
-        for (int s = warp; s < nG; s += F32_WARPS) {
-            const float2 c = sm.phi[s * 32 + lane];
-            float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int j = gp[s]; j < gp[s + 1]; ++j) {
-                const float2 v = sm.phi[I.gs_nbr[j] * 32 + lane];
-                const float ax = I.gs_ax[j], ay = I.gs_ay[j];
-                const float dg = v.x - c.x, dh = v.y - c.y;
-                g.x = fmaf(ax, dg, g.x);
-                g.y = fmaf(ay, dg, g.y);
-                g.z = fmaf(ax, dh, g.z);
-                g.w = fmaf(ay, dh, g.w);
-            }
-            sm.G[s * 32 + lane] = g;
-        }
-    } else {
-        for (int s = warp; s < nG; s += F32_WARPS) sm.G[s * 32 + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int *gp = I.gs_ptr + I.tile_gsp_off[tile];
+    const int e0 = gp[0];
+    for (int s = threadIdx.x; s < nS; s += kT) sm.slot_cell[s] = I.slot_cell[sbase + s];
+    for (int s = threadIdx.x; s <= nG; s += kT) sm.gptr[s] = (unsigned short)(gp[s] - e0);
+    const int ne = gp[nG] - e0;
+    for (int j = threadIdx.x; j < ne; j += kT) {
+        sm.gnbr[j] = I.gs_nbr[e0 + j];
+        sm.ga[j] = make_float2(I.gs_ax[e0 + j], I.gs_ay[e0 + j]);
     }
-    __syncthreads();
+    if (threadIdx.x == 0) {
+        sm.nS = nS;
+        sm.nG = nG;
+    }
+}
+
+// Warp 0 issues the bulk copies of chunk `ch` into phi[buf].
+__device__ __forceinline__ void issue_chunk(const float2 *S, int NVp, int ch, int buf, TileSmem &sm) {
+    const int lane = threadIdx.x & 31;
+    const int nS = sm.nS;
+    if (lane == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&sm.mbar[buf], (unsigned)nS * 256u);
+    }
+    __syncwarp();
+    for (int s = lane; s < nS; s += 32)
+        bulk_load(&sm.phi[buf][s * 32], S + (size_t)sm.slot_cell[s] * NVp + (size_t)ch * 32, 256u, &sm.mbar[buf]);
+}
+
+// Gradients of the first nG slots from phi[buf].
+__device__ __forceinline__ void gradients(const TileSmem &sm, int buf, int gradient_on, TileSmem &out) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nG = sm.nG;
+    const float2 *phi = sm.phi[buf];
+    for (int s = warp; s < nG; s += F32_WARPS) {
+        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (gradient_on) {
+            const float2 c = phi[s * 32 + lane];
+            for (int j = sm.gptr[s]; j < sm.gptr[s + 1]; ++j) {
+                const float2 v = phi[sm.gnbr[j] * 32 + lane];
+                const float2 a = sm.ga[j];
+                const float dg = v.x - c.x, dh = v.y - c.y;
+                g.x = fmaf(a.x, dg, g.x);
+                g.y = fmaf(a.y, dg, g.y);
+                g.z = fmaf(a.x, dh, g.z);
+                g.w = fmaf(a.y, dh, g.w);
+            }
+        }
+        out.G[s * 32 + lane] = g;
+    }
 }
 
 // Half-step reconstruction from slot s: phi + (d - xi dt/2) . grad   (g and h)
-__device__ __forceinline__ float2 recon(const Smem &sm, int s, float2 d, float hx, float hy) {
+__device__ __forceinline__ float2 recon(const TileSmem &sm, int buf, int s, float2 d, float hx, float hy) {
     const int lane = threadIdx.x & 31;
-    const float2 v = sm.phi[s * 32 + lane];
+    const float2 v = sm.phi[buf][s * 32 + lane];
     const float4 g = sm.G[s * 32 + lane];
     const float ax = d.x - hx, ay = d.y - hy;
     return make_float2(fmaf(ax, g.x, fmaf(ay, g.y, v.x)), fmaf(ax, g.z, fmaf(ay, g.w, v.y)));
 }
 
-// Face value from the upwind side(s), gradient off: plain upwind (cdugks_shakhov.cpp:277-298).
-__device__ __forceinline__ float2 face_bar(const F32Inst &I, const Smem &sm, int f, int cls, int os, int ns, float hx,
-                                           float hy) {
-    if (cls == 0) return recon(sm, os, I.fdo[f], hx, hy);
-    if (cls == 1) return recon(sm, ns, I.fdn[f], hx, hy);
-    const float2 a = recon(sm, os, I.fdo[f], hx, hy), b = recon(sm, ns, I.fdn[f], hx, hy);
+__device__ __forceinline__ float2 face_bar(const TileSmem &sm, int buf, int cls, int os, int ns, float2 fdo,
+                                           float2 fdn, float hx, float hy) {
+    if (cls == 0) return recon(sm, buf, os, fdo, hx, hy);
+    if (cls == 1) return recon(sm, buf, ns, fdn, hx, hy);
+    const float2 a = recon(sm, buf, os, fdo, hx, hy), b = recon(sm, buf, ns, fdn, hx, hy);
     return make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
+}
+
+// Sum of 16 values over the warp by halving exchanges: lane l ends with the total of value l >> 1.
+__device__ __forceinline__ float warp_sum16(float (&v)[16], int lane) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const bool up = lane & 16;
+        const float send = up ? v[k] : v[k + 8];
+        const float keep = up ? v[k + 8] : v[k];
+        v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const bool up = lane & 8;
+        const float send = up ? v[k] : v[k + 4];
+        const float keep = up ? v[k + 4] : v[k];
+        v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const bool up = lane & 4;
+        const float send = up ? v[k] : v[k + 2];
+        const float keep = up ? v[k + 2] : v[k];
+        v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    {
+        const bool up = lane & 2;
+        const float send = up ? v[0] : v[1];
+        const float keep = up ? v[1] : v[0];
+        v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    }
+    return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
+// Records a timed-out wait; the CTA then drains its own copies (bounded) and leaves the kernel.
+__device__ __forceinline__ bool wait_or_bail(TileSmem &sm, int buf, unsigned parity, DStatus *st) {
+    const bool ok = mbar_wait(&sm.mbar[buf], parity);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicExch(&st->timeout, 1);
+        mbar_wait(&sm.mbar[buf], parity);
+        mbar_wait(&sm.mbar[buf ^ 1], parity ^ 1u);
+        return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void init_barriers(TileSmem &sm) {
+    if (threadIdx.x == 0) {
+        mbar_init(&sm.mbar[0], 1);
+        mbar_init(&sm.mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
 }
 
 // =============================================================================
 // P1: raw face moments
 // =============================================================================
-__global__ void __launch_bounds__(kT, 2) k32_moments(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
+__global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
                                                     int nitems, int cur) {
     extern __shared__ float4 smem_raw[];
-    const Smem sm = smem_layout(smem_raw);
+    TileSmem &sm = *reinterpret_cast<TileSmem *>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    init_barriers(sm);
+    unsigned uses[2] = {0u, 0u};
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 item = items[it];
         const F32Inst &I = insts[item.x];
@@ -188,40 +324,66 @@ __global__ void __launch_bounds__(kT, 2) k32_moments(const F32Inst *__restrict__
         const int fs = I.tile_fstart[tile], nOF = I.tile_fstart[tile + 1] - fs;
         const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
         const int ch0 = grp * cpg, ch1 = min(I.chunks, ch0 + cpg);
-        const float2 *S = I.S[cur];
+        if (ch0 >= ch1) continue;
+        const float2 *__restrict__ S = I.S[cur];
+        const int NVp = I.NVp;
         const float hdt = (float)I.hdt;
-        for (int k = threadIdx.x; k < nOF * 22; k += kT) sm.acc[k] = 0.f;
+        const int grad_on = I.gradient;
+        const float *__restrict__ xi32x = I.xi32x;
+        const float *__restrict__ xi32y = I.xi32y;
+        const float *__restrict__ w32 = I.w32;
+        float2 *__restrict__ bnd_in = I.bnd_in;
+        stage_common(I, tile, sm);
+        for (int f = threadIdx.x; f < nOF; f += kT) {
+            const int g = fs + f;
+            OwnedFace o;
+            o.n = I.fn32[g];
+            o.fdo = I.fdo[g];
+            o.fdn = I.fdn[g];
+            const float2 uo = I.u32[I.fown[g]], un = I.u32[I.fnei[g]];
+            o.u0 = make_float2(0.5f * (uo.x + un.x), 0.5f * (uo.y + un.y));
+            o.bnd = I.fbnd[g];
+            o.face = g;
+            o.os = I.face_own_slot[g];
+            o.ns = I.face_nei_slot[g];
+            o.pad = 0;
+            sm.u.p1.of[f] = o;
+        }
+        for (int k = threadIdx.x; k < nOF * 22; k += kT) sm.u.p1.acc[k] = 0.f;
+        __syncthreads();
+        if (warp == 0) issue_chunk(S, NVp, ch0, 0, sm);
         for (int ch = ch0; ch < ch1; ++ch) {
+            const int buf = (ch - ch0) & 1;
+            if (warp == 0 && ch + 1 < ch1) issue_chunk(S, NVp, ch + 1, buf ^ 1, sm);
+            if (!wait_or_bail(sm, buf, uses[buf] & 1u, I.status)) return;
+            ++uses[buf];
+            gradients(sm, buf, grad_on, sm);
+            __syncthreads();
             const int p = ch * 32 + lane;
-            stage_chunk(I, S, tile, p, sm);
-            const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
+            const float xx = xi32x[p], xy = xi32y[p], w = w32[p];
             const float hx = hdt * xx, hy = hdt * xy;
             for (int fl = warp; fl < nOF; fl += F32_WARPS) {
-                const int f = fs + fl;
-                const int os = I.face_own_slot[f], ns = I.face_nei_slot[f];
-                const float2 n = I.fn32[f];
-                const int cls = classify(I, f, p, fmaf(n.x, xx, n.y * xy), xx, xy);
-                const float2 gb = face_bar(I, sm, f, cls, os, ns, hx, hy);
-                const int b = I.fbnd[f];
-                if (b >= 0) I.bnd_in[(size_t)b * I.NVp + p] = gb;
-                const float2 uo = I.u32[I.fown[f]], un = I.u32[I.fnei[f]];
-                const float c0x = xx - 0.5f * (uo.x + un.x), c0y = xy - 0.5f * (uo.y + un.y);
+                const OwnedFace &o = sm.u.p1.of[fl];
+                const int cls = classify(I, o.face, p, fmaf(o.n.x, xx, o.n.y * xy), xx, xy);
+                const float2 gb = face_bar(sm, buf, cls, o.os, o.ns, o.fdo, o.fdn, hx, hy);
+                if (o.bnd >= 0) bnd_in[(size_t)o.bnd * NVp + p] = gb;
+                const float c0x = xx - o.u0.x, c0y = xy - o.u0.y;
                 const float wg = w * gb.x, wh = w * gb.y;
                 const float cc = fmaf(c0x, c0x, c0y * c0y);
-                float m[F32_NMOM] = {wg,           c0x * wg,      c0y * wg,      c0x * c0x * wg,
-                                     c0x * c0y * wg, c0y * c0y * wg, c0x * cc * wg, c0y * cc * wg,
-                                     wh,           c0x * wh,      c0y * wh};
-                warp_sum(m);
-                if (lane < F32_NMOM) {
-                    float *a = sm.acc + fl * 22 + 2 * lane;
-                    kahan(a[0], a[1], pick(m, lane));
+                const float a = c0x * wg, b = c0y * wg;
+                float m[16] = {wg, a, b, c0x * a, c0x * b, c0y * b, cc * a, cc * b, wh, c0x * wh, c0y * wh,
+                               0.f, 0.f, 0.f, 0.f, 0.f};
+                const float tot = warp_sum16(m, lane);
+                if ((lane & 1) == 0 && (lane >> 1) < F32_NMOM) {
+                    float *acc = sm.u.p1.acc + fl * 22 + 2 * (lane >> 1);
+                    kahan(acc[0], acc[1], tot);
                 }
             }
             __syncthreads();
         }
         double *out = I.fpart + ((size_t)grp * I.F + fs) * F32_NMOM;
         for (int k = threadIdx.x; k < nOF * F32_NMOM; k += kT)
-            out[k] = (double)sm.acc[2 * k] - (double)sm.acc[2 * k + 1];
+            out[k] = (double)sm.u.p1.acc[2 * k] - (double)sm.u.p1.acc[2 * k + 1];
         __syncthreads();
     }
 }
@@ -426,7 +588,7 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
         } else if (type == MESO_BC_SYMMETRY) {
             mode = 4;
         }
-        double rho_w = 0.0;
+        double rho_w = 0.0, den_w = 0.0;
         if (mode == 2 || mode == 3) {
             double T_w = 0.0;
             if (mk.temperature_type == MESO_PATCH_ZERO_GRADIENT) T_w = I.T[nb];
@@ -450,6 +612,7 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
             const double num = block_sum((double)s0 - (double)c0, sh);
             const double den = block_sum((double)s1 - (double)c1, sh);
             rho_w = num / den;
+            den_w = den;
             rr = rho_w;
             TT = mk.temperature;
             uux = mk.velocity[0];
@@ -465,8 +628,9 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
             const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
             const float d = fmaf(n.x, xx, n.y * xy);
             float2 v = bin[p];
+            int cls = 0;
             if (mode != 0 && p < I.NV) {
-                const int cls = classify(I, f, p, d, xx, xy);
+                cls = classify(I, f, p, d, xx, xy);
                 if (mode == 4) {
                     const float2 r = bin[I.sym[3 * p + dir]];
                     if (cls == 1) v = r;
@@ -490,13 +654,16 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
             // moment fluxes of the final face values along n0
             const float wkn = w * d;
             const float a = wkn * v.x;
-            kahan(s[0], cc4[0], a);
+            // diffuse wall: the incoming mass flux is rho_w * den exactly (added below in FP64), so
+            // the face carries no net mass in FP32 storage either (cdugks_shakhov.cpp:468-497)
+            if (!(mode == 2 && cls == 1)) kahan(s[0], cc4[0], a);
             kahan(s[1], cc4[1], a * xx);
             kahan(s[2], cc4[2], a * xy);
             kahan(s[3], cc4[3], wkn * fmaf(fmaf(xx, xx, xy * xy), v.x, v.y));
         }
         double tot[4];
         for (int q = 0; q < 4; ++q) tot[q] = block_sum((double)s[q] - (double)cc4[q], sh);
+        if (mode == 2) tot[0] -= rho_w * den_w;
         if (threadIdx.x == 0) {
             double *o = I.fsum + (size_t)f * 4;
             for (int q = 0; q < 4; ++q) o[q] = tot[q];
@@ -610,11 +777,13 @@ __global__ void k32_cell_macros(const F32Inst *__restrict__ insts, const int *__
 // =============================================================================
 // P2: face values, flux, evolution, heat-flux partials
 // =============================================================================
-__global__ void __launch_bounds__(kT, 2) k32_update(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
+__global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
                                                    int nitems, int cur) {
     extern __shared__ float4 smem_raw[];
-    const Smem sm = smem_layout(smem_raw);
+    TileSmem &sm = *reinterpret_cast<TileSmem *>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    init_barriers(sm);
+    unsigned uses[2] = {0u, 0u};
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 item = items[it];
         const F32Inst &I = insts[item.x];
@@ -623,36 +792,74 @@ __global__ void __launch_bounds__(kT, 2) k32_update(const F32Inst *__restrict__ 
         const int cs = I.tile_cstart[tile], nc = I.tile_ncell[tile];
         const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
         const int ch0 = grp * cpg, ch1 = min(I.chunks, ch0 + cpg);
-        const float2 *S = I.S[cur];
-        float2 *Sn = I.S[cur ^ 1];
+        if (ch0 >= ch1) continue;
+        const float2 *__restrict__ S = I.S[cur];
+        float2 *__restrict__ Sn = I.S[cur ^ 1];
+        const int NVp = I.NVp;
         const float hdt = (float)I.hdt;
         const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
-        const size_t NVp = (size_t)I.NVp;
-        for (int k = threadIdx.x; k < nc * 4; k += kT) sm.acc[k] = 0.f;
+        const int grad_on = I.gradient;
+        const float *__restrict__ xi32x = I.xi32x;
+        const float *__restrict__ xi32y = I.xi32y;
+        const float *__restrict__ w32 = I.w32;
+        const float2 *__restrict__ bnd_out = I.bnd_out;
+        stage_common(I, tile, sm);
+        // tile cells: evolution constants and their faces
+        const int j0 = I.cf_ptr[cs];
+        for (int c = threadIdx.x; c < nc; c += kT) sm.u.p2.ck[c] = I.ck[cs + c];
+        for (int c = threadIdx.x; c <= nc; c += kT) sm.u.p2.cf_off[c] = I.cf_ptr[cs + c] - j0;
+        const int ncf = I.cf_ptr[cs + nc] - j0;
+        for (int e = threadIdx.x; e < ncf; e += kT) {
+            const int j = j0 + e;
+            const int f = I.cf_face[j];
+            // owner test: the cell whose face list holds entry j
+            int lo = 0, hi = nc;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (I.cf_ptr[cs + mid] <= j) lo = mid;
+                else hi = mid;
+            }
+            const bool own = I.fown[f] == cs + lo;
+            CellFace x;
+            x.n = I.fn32[f];
+            x.fdo = I.fdo[f];
+            x.fdn = I.fdn[f];
+            x.area_s = own ? I.farea[f] : -I.farea[f];
+            x.bnd = I.fbnd[f];
+            x.face = f;
+            x.oslot = I.cf_oslot[j];
+            x.own = own ? 1 : 0;
+            x.pad = 0;
+            if (x.bnd < 0) x.fk = I.fk[f];
+            sm.u.p2.cf[e] = x;
+        }
+        for (int k = threadIdx.x; k < nc * 4; k += kT) sm.u.p2.acc[k] = 0.f;
+        __syncthreads();
+        if (warp == 0) issue_chunk(S, NVp, ch0, 0, sm);
         for (int ch = ch0; ch < ch1; ++ch) {
+            const int buf = (ch - ch0) & 1;
+            if (warp == 0 && ch + 1 < ch1) issue_chunk(S, NVp, ch + 1, buf ^ 1, sm);
+            if (!wait_or_bail(sm, buf, uses[buf] & 1u, I.status)) return;
+            ++uses[buf];
+            gradients(sm, buf, grad_on, sm);
+            __syncthreads();
             const int p = ch * 32 + lane;
-            stage_chunk(I, S, tile, p, sm);
-            const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
+            const float xx = xi32x[p], xy = xi32y[p], w = w32[p];
             const float hx = hdt * xx, hy = hdt * xy;
             for (int cl = warp; cl < nc; cl += F32_WARPS) {
-                const int c = cs + cl;
                 float fg = 0.f, fh = 0.f;
-                for (int j = I.cf_ptr[c]; j < I.cf_ptr[c + 1]; ++j) {
-                    const int f = I.cf_face[j];
-                    const bool own = I.fown[f] == c;
-                    const float2 n = I.fn32[f];
-                    const float d = fmaf(n.x, xx, n.y * xy);
-                    const float knA = (own ? d : -d) * I.farea[f];
-                    const int b = I.fbnd[f];
+                for (int e = sm.u.p2.cf_off[cl]; e < sm.u.p2.cf_off[cl + 1]; ++e) {
+                    const CellFace &x = sm.u.p2.cf[e];
+                    const float d = fmaf(x.n.x, xx, x.n.y * xy);
+                    const float knA = d * x.area_s;
                     float2 gf;
-                    if (b >= 0) {
-                        gf = I.bnd_out[(size_t)b * NVp + p];
+                    if (x.bnd >= 0) {
+                        gf = bnd_out[(size_t)x.bnd * NVp + p];
                     } else {
-                        const int o = I.cf_oslot[j];
-                        const int os = own ? cl : o, ns = own ? o : cl;
-                        const int cls = classify(I, f, p, d, xx, xy);
-                        const float2 gb = face_bar(I, sm, f, cls, os, ns, hx, hy);
-                        const FaceK k = I.fk[f];
+                        const int os = x.own ? cl : x.oslot, ns = x.own ? x.oslot : cl;
+                        const int cls = classify(I, x.face, p, d, xx, xy);
+                        const float2 gb = face_bar(sm, buf, cls, os, ns, x.fdo, x.fdn, hx, hy);
+                        const FaceK &k = x.fk;
                         const float2 gs = shakhov(xx - k.ux, xy - k.uy, k.A, k.bl, k.qx, k.qy, k.sg, k.sh, k.iRT, k.hm,
                                                   k3, twoK);
                         gf = make_float2(fmaf(k.oCs, gb.x, k.Cs * gs.x), fmaf(k.oCs, gb.y, k.Cs * gs.y));
@@ -660,8 +867,8 @@ __global__ void __launch_bounds__(kT, 2) k32_update(const F32Inst *__restrict__ 
                     fg = fmaf(knA, gf.x, fg);
                     fh = fmaf(knA, gf.y, fh);
                 }
-                const CellK k = I.ck[c];
-                const float2 old = sm.phi[cl * 32 + lane];
+                const CellK &k = sm.u.p2.ck[cl];
+                const float2 old = sm.phi[buf][cl * 32 + lane];
                 // state n (cdugks_shakhov.cpp:673-680)
                 const float2 sn = shakhov(xx - k.unx, xy - k.uny, k.An, k.bln, k.qnx, k.qny, k.sgn, k.shn, k.iRTn,
                                           k.hmn, k3, twoK);
@@ -673,13 +880,13 @@ __global__ void __launch_bounds__(kT, 2) k32_update(const F32Inst *__restrict__ 
                 // evolution (:689-690)
                 const float g = k.C * (gn + k.hdt_tau * s1.x + k.hdt_taun * (sn.x - gn) - k.dt_v * fg);
                 const float h = k.C * (hn + k.hdt_tau * s1.y + k.hdt_taun * (sn.y - hn) - k.dt_v * fh);
-                // heat flux partial (:692) and f-bar-plus (:694-695)
+                Sn[(size_t)(cs + cl) * NVp + p] = make_float2(fmaf(k.Cs, s1.x - g, g), fmaf(k.Cs, s1.y - h, h));
+                // heat-flux partial (:692)
                 const float hw = 0.5f * w * fmaf(fmaf(cx, cx, cy * cy), g, h);
                 float qv[2] = {hw * cx, hw * cy};
-                Sn[(size_t)c * NVp + p] = make_float2(fmaf(k.Cs, s1.x - g, g), fmaf(k.Cs, s1.y - h, h));
                 warp_sum(qv);
                 if (lane < 2) {
-                    float *a = sm.acc + cl * 4 + 2 * lane;
+                    float *a = sm.u.p2.acc + cl * 4 + 2 * lane;
                     kahan(a[0], a[1], lane == 0 ? qv[0] : qv[1]);
                 }
             }
@@ -687,8 +894,8 @@ __global__ void __launch_bounds__(kT, 2) k32_update(const F32Inst *__restrict__ 
         }
         for (int k = threadIdx.x; k < nc * 2; k += kT) {
             const int cl = k >> 1, comp = k & 1;
-            I.qpart[((size_t)grp * I.C + cs + cl) * 2 + comp] = (double)sm.acc[cl * 4 + 2 * comp] -
-                                                                  (double)sm.acc[cl * 4 + 2 * comp + 1];
+            I.qpart[((size_t)grp * I.C + cs + cl) * 2 + comp] =
+                (double)sm.u.p2.acc[cl * 4 + 2 * comp] - (double)sm.u.p2.acc[cl * 4 + 2 * comp + 1];
         }
         __syncthreads();
     }
@@ -832,9 +1039,9 @@ int grid_of(int total, int per_block, int cap) {
 
 int fp32_configure(int device) {
     (void)device;
-    if (cudaFuncSetAttribute(k32_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) != cudaSuccess)
+    if (cudaFuncSetAttribute(k32_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem) != cudaSuccess)
         return -1;
-    if (cudaFuncSetAttribute(k32_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) != cudaSuccess)
+    if (cudaFuncSetAttribute(k32_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem) != cudaSuccess)
         return -1;
     return 0;
 }
@@ -845,12 +1052,12 @@ const char *const kFp32Phases[] = {"k32_moments", "k32_face_macros", "k32_face_e
 int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev) {
     const int sms = s.num_sms;
     const int cap = sms * 32;
-    const int tile_grid = s.nitems < sms * 2 ? s.nitems : sms * 2;
+    const int tile_grid = s.nitems < sms ? s.nitems : sms;  // one persistent CTA per SM
     auto mark = [&](int k) {
         if (ev) cudaEventRecord(ev[k], stream);
     };
     mark(0);
-    k32_moments<<<tile_grid, kT, kSmemBytes, stream>>>(s.d_inst, s.d_items, s.nitems, s.cur);
+    k32_moments<<<tile_grid, kT, kTileSmem, stream>>>(s.d_inst, s.d_items, s.nitems, s.cur);
     mark(1);
     k32_face_macros<<<grid_of(s.total_faces, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
                                                                           s.total_faces);
@@ -867,7 +1074,7 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     k32_cell_macros<<<grid_of(s.total_cells, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_cell_items, s.ninst,
                                                                           s.total_cells);
     mark(5);
-    k32_update<<<tile_grid, kT, kSmemBytes, stream>>>(s.d_inst, s.d_items, s.nitems, s.cur);
+    k32_update<<<tile_grid, kT, kTileSmem, stream>>>(s.d_inst, s.d_items, s.nitems, s.cur);
     mark(6);
     k32_heat_flux<<<grid_of(s.total_cells, 256, cap), 256, 0, stream>>>(s.d_inst, s.d_cell_items, s.ninst,
                                                                         s.total_cells, 1);

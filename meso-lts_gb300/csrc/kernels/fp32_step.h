@@ -15,11 +15,13 @@ namespace meso {
 
 // Kernel limits (the tile planner shrinks tiles until every tile fits).
 constexpr int F32_LANES = 32;       // velocities per chunk (one per lane)
-constexpr int F32_WARPS = 8;        // warps per CTA
+constexpr int F32_WARPS = 16;       // warps per CTA of the tile kernels
 constexpr int F32_MAX_SLOTS = 160;  // tile + two-ring halo cells
 constexpr int F32_MAX_GSLOTS = 112; // tile + one-ring halo cells (gradients)
+constexpr int F32_MAX_GENT = 640;   // gradient stencil entries per tile
 constexpr int F32_MAX_OWNED = 144;  // faces owned by a tile
 constexpr int F32_MAX_CELLS = 64;   // cells per tile
+constexpr int F32_MAX_CF = 256;     // cell-face entries per tile (tile cells x faces per cell)
 constexpr int F32_NMOM = 11;        // raw face moments about the reference velocity (2-D)
 
 // Face equilibrium scalars for FP32 evaluation of g_S, h_S at a face.
