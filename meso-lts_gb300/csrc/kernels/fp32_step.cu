@@ -623,6 +623,9 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
         const float ux = (float)uux, uy = (float)uuy;
         const int dir = mk.direction;
         const float au = (float)mk.alpha_u, aT = (float)mk.alpha_T;
+        // The balance and the incoming set use the same temperature only for a fixedValue wall
+        // (a zeroGradient wall balances with T_cell but sets with the patch scalar, :473-479 vs :533).
+        const bool exact_mass = mode == 2 && mk.temperature_type == MESO_PATCH_FIXED_VALUE;
         float s[4] = {0.f, 0.f, 0.f, 0.f}, cc4[4] = {0.f, 0.f, 0.f, 0.f};
         for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
             const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
@@ -656,14 +659,14 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
             const float a = wkn * v.x;
             // diffuse wall: the incoming mass flux is rho_w * den exactly (added below in FP64), so
             // the face carries no net mass in FP32 storage either (cdugks_shakhov.cpp:468-497)
-            if (!(mode == 2 && cls == 1)) kahan(s[0], cc4[0], a);
+            if (!(exact_mass && cls == 1)) kahan(s[0], cc4[0], a);
             kahan(s[1], cc4[1], a * xx);
             kahan(s[2], cc4[2], a * xy);
             kahan(s[3], cc4[3], wkn * fmaf(fmaf(xx, xx, xy * xy), v.x, v.y));
         }
         double tot[4];
         for (int q = 0; q < 4; ++q) tot[q] = block_sum((double)s[q] - (double)cc4[q], sh);
-        if (mode == 2) tot[0] -= rho_w * den_w;
+        if (exact_mass) tot[0] -= rho_w * den_w;
         if (threadIdx.x == 0) {
             double *o = I.fsum + (size_t)f * 4;
             for (int q = 0; q < 4; ++q) o[q] = tot[q];
