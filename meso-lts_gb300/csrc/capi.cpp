@@ -478,7 +478,7 @@ meso_ctx *new_ctx(const meso_mesh_desc *m, const meso_dvs_desc *d, const meso_ma
                        "FP32 storage covers the 2-D Shakhov solver without the limiter; use MESO_FP64");
             return nullptr;
         }
-        if (!plan_fp32(*m, 64, c->rn, c->plan)) {
+        if (!plan_fp32(*m, meso::F32_MAX_CELLS, c->rn, c->plan)) {
             *rc = fail(MESO_ERR_UNSUPPORTED, "mesh connectivity exceeds the FP32 tile limits");
             return nullptr;
         }

@@ -10,7 +10,7 @@
 namespace meso_host {
 
 bool plan_fp32(const meso_mesh_desc &m, int tile_cells, Renumbering &rn, TilePlan &plan) {
-    for (int T = std::min(tile_cells, meso::F32_MAX_CELLS); T >= 4; T = T * 3 / 4) {
+    for (int T = std::min(tile_cells, meso::F32_MAX_CELLS); T >= 4; T = T * 7 / 8) {
         std::vector<int> sizes;
         rn = renumber_tiled(m, T, sizes);
         if (build_tile_plan(m, rn, sizes, meso::F32_MAX_SLOTS, meso::F32_MAX_GSLOTS, meso::F32_MAX_OWNED,
@@ -24,6 +24,7 @@ bool plan_fp32(const meso_mesh_desc &m, int tile_cells, Renumbering &rn, TilePla
 int default_ngroup(int ntile, int chunks, int num_sms) {
     // ~6 (tile, group) items per persistent CTA (one per SM), groups of at least 2 chunks
     int want = (6 * num_sms + ntile - 1) / std::max(ntile, 1);
+    want = std::max(want, 1);
     want = std::max(1, std::min(want, std::max(1, chunks / 2)));
     return want;
 }
@@ -40,7 +41,8 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
     auto &A = c->arena;
     auto s = c->stream;
     const int C = m->ncell, F = m->nface, NV = d->nv;
-    const int NVp = (NV + 31) / 32 * 32;
+    const int vpl = NV >= 256 ? 2 : 1;  // small velocity sets keep one velocity per lane
+    const int NVp = (NV + 32 * vpl - 1) / (32 * vpl) * (32 * vpl);
     const auto &rn = c->rn;
     meso::F32Inst I;
     std::memset(&I, 0, sizeof(I));
@@ -49,7 +51,8 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
     I.NV = NV;
     I.NVp = NVp;
     I.ntile = P.ntile;
-    I.chunks = NVp / 32;
+    I.vpl = vpl;
+    I.chunks = NVp / (32 * vpl);
     I.ngroup = ngroup > 0 ? std::min(ngroup, I.chunks) : default_ngroup(P.ntile, I.chunks, c->num_sms);
     const meso_params &p = c->params;
     I.dt = p.dt;
@@ -203,12 +206,16 @@ int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso
         coff.push_back(coff.back() + I.C);
         boff.push_back(boff.back() + I.nb);
     }
-    // largest work first: items of big-NV instances lead the list (persistent CTAs take them in order)
+    // items of two-velocities-per-lane instances first (their own launch), then largest work first
+    // (persistent CTAs take items in order)
     std::stable_sort(items.begin(), items.end(), [&](const int2 &a, const int2 &b) {
         const auto &A = insts[a.x], &B = insts[b.x];
+        if (A.vpl != B.vpl) return A.vpl > B.vpl;
         long wa = (long)((A.chunks + A.ngroup - 1) / A.ngroup), wb = (long)((B.chunks + B.ngroup - 1) / B.ngroup);
         return wa > wb;
     });
+    int n2 = 0;
+    for (const int2 &it : items) n2 += insts[it.x].vpl == 2 ? 1 : 0;
     auto put = [&](const void *src, size_t bytes) -> void * {
         void *p = nullptr;
         if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) return nullptr;
@@ -224,6 +231,7 @@ int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso
     if (!s.d_inst || !s.d_items || !s.d_face_items || !s.d_cell_items || !s.d_bnd_items) return -1;
     s.ninst = n;
     s.nitems = (int)items.size();
+    s.nitems_vpl2 = n2;
     s.total_faces = foff.back();
     s.total_cells = coff.back();
     s.total_bnd = boff.back();

@@ -1,11 +1,14 @@
 // FP32-storage Shakhov CDUGKS step (2-D), tiled and fused.
 //
 // Storage: g, h interleaved as float2, velocity-contiguous per cell
-// ([cell][NVp], NVp = NV rounded up to 32), two buffers (state n, n+1).
+// ([cell][NVp], NVp = NV rounded up to 32 VPL), two buffers (state n, n+1).
+// VPL (velocities per lane) is 2 for velocity sets of 256 and more, 1 below:
+// a chunk is 32 VPL velocities, lane l of a warp handles velocities
+// chunk*32*VPL + v*32 + l, v < VPL.
 // A step is seven launches, each over all instances of a batch:
 //
 //   P1  k32_moments      per (tile, velocity group) CTA: stage the tile and its
-//                        two-ring halo for 32 velocities in shared memory,
+//                        two-ring halo for one chunk in shared memory,
 //                        compute every tile / 1-ring cell's least-squares
 //                        gradient once, reconstruct each owned face (half-step
 //                        upwind, cdugks_shakhov.cpp:223-276) and accumulate 11
@@ -155,10 +158,11 @@ struct CellFace {      // P2: one face of a tile cell, seen from that cell
     unsigned char own, pad;
 };
 
-struct __align__(128) TileSmem {
-    float2 phi[2][F32_MAX_SLOTS * 32];  // double-buffered chunk of the tile + halo (TMA destination)
-    float4 G[F32_MAX_GSLOTS * 32];      // gradients (g_x, g_y, h_x, h_y) of tile + 1-ring cells
-    float2 ga[F32_MAX_GENT];            // gradient stencil coefficients
+template <int VPL> struct __align__(128) TileSmem {
+    static constexpr int SEG = 32 * VPL;         // velocities of one slot in a chunk
+    float2 phi[2][F32_MAX_SLOTS * SEG];         // double-buffered chunk of the tile + halo (bulk-copy target)
+    float4 G[F32_MAX_GSLOTS * SEG];             // gradients (g_x, g_y, h_x, h_y) of tile + 1-ring cells
+    float2 ga[F32_MAX_GENT];                    // gradient stencil coefficients
     int slot_cell[F32_MAX_SLOTS];
     unsigned short gnbr[F32_MAX_GENT];
     unsigned short gptr[F32_MAX_GSLOTS + 1];
@@ -178,10 +182,11 @@ struct __align__(128) TileSmem {
     } u;
 };
 
-constexpr size_t kTileSmem = sizeof(TileSmem);
+template <int VPL> constexpr size_t tile_smem() { return sizeof(TileSmem<VPL>); }
+static_assert(sizeof(TileSmem<F32_MAX_VPL>) <= 227 * 1024, "tile staging exceeds the shared memory of one CTA");
 
-// Common per-item staging of the slot list and the gradient stencil.
-__device__ __forceinline__ void stage_common(const F32Inst &I, int tile, TileSmem &sm) {
+// Per-item staging of the slot list and the gradient stencil.
+template <int VPL> __device__ __forceinline__ void stage_common(const F32Inst &I, int tile, TileSmem<VPL> &sm) {
     const int sbase = I.tile_slot_ptr[tile];
     const int nS = I.tile_slot_ptr[tile + 1] - sbase;
     const int nG = I.tile_gslots[tile];
@@ -200,56 +205,73 @@ __device__ __forceinline__ void stage_common(const F32Inst &I, int tile, TileSme
     }
 }
 
-// Warp 0 issues the bulk copies of chunk `ch` into phi[buf].
-__device__ __forceinline__ void issue_chunk(const float2 *S, int NVp, int ch, int buf, TileSmem &sm) {
+// Warp 0 issues the bulk copies of chunk `ch` (32 VPL velocities of every slot) into phi[buf].
+template <int VPL>
+__device__ __forceinline__ void issue_chunk(const float2 *S, int NVp, int ch, int buf, TileSmem<VPL> &sm) {
+    constexpr int SEG = TileSmem<VPL>::SEG;
     const int lane = threadIdx.x & 31;
     const int nS = sm.nS;
     if (lane == 0) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(&sm.mbar[buf], (unsigned)nS * 256u);
+        mbar_expect_tx(&sm.mbar[buf], (unsigned)nS * (unsigned)(SEG * 8));
     }
     __syncwarp();
     for (int s = lane; s < nS; s += 32)
-        bulk_load(&sm.phi[buf][s * 32], S + (size_t)sm.slot_cell[s] * NVp + (size_t)ch * 32, 256u, &sm.mbar[buf]);
+        bulk_load(&sm.phi[buf][s * SEG], S + (size_t)sm.slot_cell[s] * NVp + (size_t)ch * SEG, SEG * 8u,
+                  &sm.mbar[buf]);
 }
 
 // Gradients of the first nG slots from phi[buf].
-__device__ __forceinline__ void gradients(const TileSmem &sm, int buf, int gradient_on, TileSmem &out) {
+template <int VPL> __device__ __forceinline__ void gradients(TileSmem<VPL> &sm, int buf, int gradient_on) {
+    constexpr int SEG = TileSmem<VPL>::SEG;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nG = sm.nG;
     const float2 *phi = sm.phi[buf];
     for (int s = warp; s < nG; s += F32_WARPS) {
-        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 g[VPL];
+        float2 c[VPL];
+#pragma unroll
+        for (int v = 0; v < VPL; ++v) {
+            g[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+            c[v] = phi[s * SEG + v * 32 + lane];
+        }
         if (gradient_on) {
-            const float2 c = phi[s * 32 + lane];
             for (int j = sm.gptr[s]; j < sm.gptr[s + 1]; ++j) {
-                const float2 v = phi[sm.gnbr[j] * 32 + lane];
+                const int nb = sm.gnbr[j] * SEG + lane;
                 const float2 a = sm.ga[j];
-                const float dg = v.x - c.x, dh = v.y - c.y;
-                g.x = fmaf(a.x, dg, g.x);
-                g.y = fmaf(a.y, dg, g.y);
-                g.z = fmaf(a.x, dh, g.z);
-                g.w = fmaf(a.y, dh, g.w);
+#pragma unroll
+                for (int v = 0; v < VPL; ++v) {
+                    const float2 x = phi[nb + v * 32];
+                    const float dg = x.x - c[v].x, dh = x.y - c[v].y;
+                    g[v].x = fmaf(a.x, dg, g[v].x);
+                    g[v].y = fmaf(a.y, dg, g[v].y);
+                    g[v].z = fmaf(a.x, dh, g[v].z);
+                    g[v].w = fmaf(a.y, dh, g[v].w);
+                }
             }
         }
-        out.G[s * 32 + lane] = g;
+#pragma unroll
+        for (int v = 0; v < VPL; ++v) sm.G[s * SEG + v * 32 + lane] = g[v];
     }
 }
 
-// Half-step reconstruction from slot s: phi + (d - xi dt/2) . grad   (g and h)
-__device__ __forceinline__ float2 recon(const TileSmem &sm, int buf, int s, float2 d, float hx, float hy) {
-    const int lane = threadIdx.x & 31;
-    const float2 v = sm.phi[buf][s * 32 + lane];
-    const float4 g = sm.G[s * 32 + lane];
+// Half-step reconstruction from slot s, velocity v of the lane: phi + (d - xi dt/2) . grad  (g and h)
+template <int VPL>
+__device__ __forceinline__ float2 recon(const TileSmem<VPL> &sm, int buf, int s, int v, float2 d, float hx, float hy) {
+    constexpr int SEG = TileSmem<VPL>::SEG;
+    const int k = s * SEG + v * 32 + (threadIdx.x & 31);
+    const float2 x = sm.phi[buf][k];
+    const float4 g = sm.G[k];
     const float ax = d.x - hx, ay = d.y - hy;
-    return make_float2(fmaf(ax, g.x, fmaf(ay, g.y, v.x)), fmaf(ax, g.z, fmaf(ay, g.w, v.y)));
+    return make_float2(fmaf(ax, g.x, fmaf(ay, g.y, x.x)), fmaf(ax, g.z, fmaf(ay, g.w, x.y)));
 }
 
-__device__ __forceinline__ float2 face_bar(const TileSmem &sm, int buf, int cls, int os, int ns, float2 fdo,
-                                           float2 fdn, float hx, float hy) {
-    if (cls == 0) return recon(sm, buf, os, fdo, hx, hy);
-    if (cls == 1) return recon(sm, buf, ns, fdn, hx, hy);
-    const float2 a = recon(sm, buf, os, fdo, hx, hy), b = recon(sm, buf, ns, fdn, hx, hy);
+template <int VPL>
+__device__ __forceinline__ float2 face_bar(const TileSmem<VPL> &sm, int buf, int v, int cls, int os, int ns,
+                                           float2 fdo, float2 fdn, float hx, float hy) {
+    if (cls == 0) return recon(sm, buf, os, v, fdo, hx, hy);
+    if (cls == 1) return recon(sm, buf, ns, v, fdn, hx, hy);
+    const float2 a = recon(sm, buf, os, v, fdo, hx, hy), b = recon(sm, buf, ns, v, fdn, hx, hy);
     return make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
 }
 
@@ -286,7 +308,8 @@ __device__ __forceinline__ float warp_sum16(float (&v)[16], int lane) {
 }
 
 // Records a timed-out wait; the CTA then drains its own copies (bounded) and leaves the kernel.
-__device__ __forceinline__ bool wait_or_bail(TileSmem &sm, int buf, unsigned parity, DStatus *st) {
+template <int VPL>
+__device__ __forceinline__ bool wait_or_bail(TileSmem<VPL> &sm, int buf, unsigned parity, DStatus *st) {
     const bool ok = mbar_wait(&sm.mbar[buf], parity);
     if (__syncthreads_or(!ok)) {
         if (threadIdx.x == 0) atomicExch(&st->timeout, 1);
@@ -297,7 +320,7 @@ __device__ __forceinline__ bool wait_or_bail(TileSmem &sm, int buf, unsigned par
     return true;
 }
 
-__device__ __forceinline__ void init_barriers(TileSmem &sm) {
+template <int VPL> __device__ __forceinline__ void init_barriers(TileSmem<VPL> &sm) {
     if (threadIdx.x == 0) {
         mbar_init(&sm.mbar[0], 1);
         mbar_init(&sm.mbar[1], 1);
@@ -309,13 +332,15 @@ __device__ __forceinline__ void init_barriers(TileSmem &sm) {
 // =============================================================================
 // P1: raw face moments
 // =============================================================================
+template <int VPL>
 __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
                                                     int nitems, int cur) {
+    constexpr int SEG = TileSmem<VPL>::SEG;
     extern __shared__ float4 smem_raw[];
-    TileSmem &sm = *reinterpret_cast<TileSmem *>(smem_raw);
+    TileSmem<VPL> &sm = *reinterpret_cast<TileSmem<VPL> *>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     init_barriers(sm);
-    unsigned uses[2] = {0u, 0u};
+    unsigned use0 = 0u, use1 = 0u;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 item = items[it];
         const F32Inst &I = insts[item.x];
@@ -351,28 +376,52 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
         }
         for (int k = threadIdx.x; k < nOF * 22; k += kT) sm.u.p1.acc[k] = 0.f;
         __syncthreads();
-        if (warp == 0) issue_chunk(S, NVp, ch0, 0, sm);
+        if (warp == 0) issue_chunk<VPL>(S, NVp, ch0, 0, sm);
         for (int ch = ch0; ch < ch1; ++ch) {
             const int buf = (ch - ch0) & 1;
-            if (warp == 0 && ch + 1 < ch1) issue_chunk(S, NVp, ch + 1, buf ^ 1, sm);
-            if (!wait_or_bail(sm, buf, uses[buf] & 1u, I.status)) return;
-            ++uses[buf];
-            gradients(sm, buf, grad_on, sm);
+            if (warp == 0 && ch + 1 < ch1) issue_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
+            if (!wait_or_bail(sm, buf, (buf ? use1 : use0) & 1u, I.status)) return;
+            if (buf) ++use1;
+            else ++use0;
+            gradients(sm, buf, grad_on);
             __syncthreads();
-            const int p = ch * 32 + lane;
-            const float xx = xi32x[p], xy = xi32y[p], w = w32[p];
-            const float hx = hdt * xx, hy = hdt * xy;
+            float xx[VPL], xy[VPL], w[VPL], hx[VPL], hy[VPL];
+            int p[VPL];
+#pragma unroll
+            for (int v = 0; v < VPL; ++v) {
+                p[v] = ch * SEG + v * 32 + lane;
+                xx[v] = xi32x[p[v]];
+                xy[v] = xi32y[p[v]];
+                w[v] = w32[p[v]];
+                hx[v] = hdt * xx[v];
+                hy[v] = hdt * xy[v];
+            }
             for (int fl = warp; fl < nOF; fl += F32_WARPS) {
-                const OwnedFace &o = sm.u.p1.of[fl];
-                const int cls = classify(I, o.face, p, fmaf(o.n.x, xx, o.n.y * xy), xx, xy);
-                const float2 gb = face_bar(sm, buf, cls, o.os, o.ns, o.fdo, o.fdn, hx, hy);
-                if (o.bnd >= 0) bnd_in[(size_t)o.bnd * NVp + p] = gb;
-                const float c0x = xx - o.u0.x, c0y = xy - o.u0.y;
-                const float wg = w * gb.x, wh = w * gb.y;
-                const float cc = fmaf(c0x, c0x, c0y * c0y);
-                const float a = c0x * wg, b = c0y * wg;
-                float m[16] = {wg, a, b, c0x * a, c0x * b, c0y * b, cc * a, cc * b, wh, c0x * wh, c0y * wh,
-                               0.f, 0.f, 0.f, 0.f, 0.f};
+                const OwnedFace o = sm.u.p1.of[fl];
+                float m[16];
+#pragma unroll
+                for (int k = 0; k < 16; ++k) m[k] = 0.f;
+#pragma unroll
+                for (int v = 0; v < VPL; ++v) {
+                    const int cls = classify(I, o.face, p[v], fmaf(o.n.x, xx[v], o.n.y * xy[v]), xx[v], xy[v]);
+                    const float2 gb = face_bar(sm, buf, v, cls, o.os, o.ns, o.fdo, o.fdn, hx[v], hy[v]);
+                    if (o.bnd >= 0) bnd_in[(size_t)o.bnd * NVp + p[v]] = gb;
+                    const float c0x = xx[v] - o.u0.x, c0y = xy[v] - o.u0.y;
+                    const float wg = w[v] * gb.x, wh = w[v] * gb.y;
+                    const float cc = fmaf(c0x, c0x, c0y * c0y);
+                    const float a = c0x * wg, b = c0y * wg;
+                    m[0] += wg;
+                    m[1] += a;
+                    m[2] += b;
+                    m[3] = fmaf(c0x, a, m[3]);
+                    m[4] = fmaf(c0x, b, m[4]);
+                    m[5] = fmaf(c0y, b, m[5]);
+                    m[6] = fmaf(cc, a, m[6]);
+                    m[7] = fmaf(cc, b, m[7]);
+                    m[8] += wh;
+                    m[9] = fmaf(c0x, wh, m[9]);
+                    m[10] = fmaf(c0y, wh, m[10]);
+                }
                 const float tot = warp_sum16(m, lane);
                 if ((lane & 1) == 0 && (lane >> 1) < F32_NMOM) {
                     float *acc = sm.u.p1.acc + fl * 22 + 2 * (lane >> 1);
@@ -384,6 +433,161 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
         double *out = I.fpart + ((size_t)grp * I.F + fs) * F32_NMOM;
         for (int k = threadIdx.x; k < nOF * F32_NMOM; k += kT)
             out[k] = (double)sm.u.p1.acc[2 * k] - (double)sm.u.p1.acc[2 * k + 1];
+        __syncthreads();
+    }
+}
+
+// =============================================================================
+// P2: face values, flux, evolution, heat-flux partials
+// =============================================================================
+template <int VPL>
+__global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
+                                                   int nitems, int cur) {
+    constexpr int SEG = TileSmem<VPL>::SEG;
+    extern __shared__ float4 smem_raw[];
+    TileSmem<VPL> &sm = *reinterpret_cast<TileSmem<VPL> *>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    init_barriers(sm);
+    unsigned use0 = 0u, use1 = 0u;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int2 item = items[it];
+        const F32Inst &I = insts[item.x];
+        if (step_stopped(I.status)) continue;
+        const int tile = item.y / I.ngroup, grp = item.y % I.ngroup;
+        const int cs = I.tile_cstart[tile], nc = I.tile_ncell[tile];
+        const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
+        const int ch0 = grp * cpg, ch1 = min(I.chunks, ch0 + cpg);
+        if (ch0 >= ch1) continue;
+        const float2 *__restrict__ S = I.S[cur];
+        float2 *__restrict__ Sn = I.S[cur ^ 1];
+        const int NVp = I.NVp;
+        const float hdt = (float)I.hdt;
+        const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
+        const int grad_on = I.gradient;
+        const float *__restrict__ xi32x = I.xi32x;
+        const float *__restrict__ xi32y = I.xi32y;
+        const float *__restrict__ w32 = I.w32;
+        const float2 *__restrict__ bnd_out = I.bnd_out;
+        stage_common(I, tile, sm);
+        const int j0 = I.cf_ptr[cs];
+        for (int c = threadIdx.x; c < nc; c += kT) sm.u.p2.ck[c] = I.ck[cs + c];
+        for (int c = threadIdx.x; c <= nc; c += kT) sm.u.p2.cf_off[c] = I.cf_ptr[cs + c] - j0;
+        const int ncf = I.cf_ptr[cs + nc] - j0;
+        for (int e = threadIdx.x; e < ncf; e += kT) {
+            const int j = j0 + e;
+            const int f = I.cf_face[j];
+            int lo = 0, hi = nc;  // the tile cell whose face list holds entry j
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (I.cf_ptr[cs + mid] <= j) lo = mid;
+                else hi = mid;
+            }
+            const bool own = I.fown[f] == cs + lo;
+            CellFace x;
+            x.n = I.fn32[f];
+            x.fdo = I.fdo[f];
+            x.fdn = I.fdn[f];
+            x.area_s = own ? I.farea[f] : -I.farea[f];
+            x.bnd = I.fbnd[f];
+            x.face = f;
+            x.oslot = I.cf_oslot[j];
+            x.own = own ? 1 : 0;
+            x.pad = 0;
+            if (x.bnd < 0) x.fk = I.fk[f];
+            sm.u.p2.cf[e] = x;
+        }
+        for (int k = threadIdx.x; k < nc * 4; k += kT) sm.u.p2.acc[k] = 0.f;
+        __syncthreads();
+        if (warp == 0) issue_chunk<VPL>(S, NVp, ch0, 0, sm);
+        for (int ch = ch0; ch < ch1; ++ch) {
+            const int buf = (ch - ch0) & 1;
+            if (warp == 0 && ch + 1 < ch1) issue_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
+            if (!wait_or_bail(sm, buf, (buf ? use1 : use0) & 1u, I.status)) return;
+            if (buf) ++use1;
+            else ++use0;
+            gradients(sm, buf, grad_on);
+            __syncthreads();
+            float xx[VPL], xy[VPL], w[VPL], hx[VPL], hy[VPL];
+            int p[VPL];
+#pragma unroll
+            for (int v = 0; v < VPL; ++v) {
+                p[v] = ch * SEG + v * 32 + lane;
+                xx[v] = xi32x[p[v]];
+                xy[v] = xi32y[p[v]];
+                w[v] = w32[p[v]];
+                hx[v] = hdt * xx[v];
+                hy[v] = hdt * xy[v];
+            }
+            for (int cl = warp; cl < nc; cl += F32_WARPS) {
+                float fg[VPL], fh[VPL];
+#pragma unroll
+                for (int v = 0; v < VPL; ++v) fg[v] = fh[v] = 0.f;
+                const int e1 = sm.u.p2.cf_off[cl + 1];
+                for (int e = sm.u.p2.cf_off[cl]; e < e1; ++e) {
+                    const CellFace &x = sm.u.p2.cf[e];
+                    const float2 n = x.n;
+                    const float area_s = x.area_s;
+                    if (x.bnd >= 0) {
+                        const float2 *bo = bnd_out + (size_t)x.bnd * NVp;
+#pragma unroll
+                        for (int v = 0; v < VPL; ++v) {
+                            const float knA = fmaf(n.x, xx[v], n.y * xy[v]) * area_s;
+                            const float2 gf = bo[p[v]];
+                            fg[v] = fmaf(knA, gf.x, fg[v]);
+                            fh[v] = fmaf(knA, gf.y, fh[v]);
+                        }
+                    } else {
+                        const int os = x.own ? cl : x.oslot, ns = x.own ? x.oslot : cl;
+                        const FaceK k = x.fk;
+                        const float2 fdo = x.fdo, fdn = x.fdn;
+#pragma unroll
+                        for (int v = 0; v < VPL; ++v) {
+                            const float d = fmaf(n.x, xx[v], n.y * xy[v]);
+                            const int cls = classify(I, x.face, p[v], d, xx[v], xy[v]);
+                            const float2 gb = face_bar(sm, buf, v, cls, os, ns, fdo, fdn, hx[v], hy[v]);
+                            const float2 gs = shakhov(xx[v] - k.ux, xy[v] - k.uy, k.A, k.bl, k.qx, k.qy, k.sg, k.sh,
+                                                      k.iRT, k.hm, k3, twoK);
+                            const float knA = d * area_s;
+                            fg[v] = fmaf(knA, fmaf(k.oCs, gb.x, k.Cs * gs.x), fg[v]);
+                            fh[v] = fmaf(knA, fmaf(k.oCs, gb.y, k.Cs * gs.y), fh[v]);
+                        }
+                    }
+                }
+                const CellK k = sm.u.p2.ck[cl];
+                float qv[2] = {0.f, 0.f};
+#pragma unroll
+                for (int v = 0; v < VPL; ++v) {
+                    const float2 old = sm.phi[buf][cl * SEG + v * 32 + lane];
+                    // state n (cdugks_shakhov.cpp:673-680)
+                    const float2 sn = shakhov(xx[v] - k.unx, xy[v] - k.uny, k.An, k.bln, k.qnx, k.qny, k.sgn, k.shn,
+                                              k.iRTn, k.hmn, k3, twoK);
+                    const float gn = fmaf(k.cm, sn.x - old.x, old.x);
+                    const float hn = fmaf(k.cm, sn.y - old.y, old.y);
+                    // state n+1 with q at n (:682-687)
+                    const float cx = xx[v] - k.ux, cy = xy[v] - k.uy;
+                    const float2 s1 = shakhov(cx, cy, k.A, k.bl, k.qnx, k.qny, k.sg, k.sh, k.iRT, k.hm, k3, twoK);
+                    // evolution (:689-690)
+                    const float g = k.C * (gn + k.hdt_tau * s1.x + k.hdt_taun * (sn.x - gn) - k.dt_v * fg[v]);
+                    const float h = k.C * (hn + k.hdt_tau * s1.y + k.hdt_taun * (sn.y - hn) - k.dt_v * fh[v]);
+                    Sn[(size_t)(cs + cl) * NVp + p[v]] = make_float2(fmaf(k.Cs, s1.x - g, g), fmaf(k.Cs, s1.y - h, h));
+                    // heat-flux partial (:692)
+                    const float hw = 0.5f * w[v] * fmaf(fmaf(cx, cx, cy * cy), g, h);
+                    qv[0] = fmaf(hw, cx, qv[0]);
+                    qv[1] = fmaf(hw, cy, qv[1]);
+                }
+                warp_sum(qv);
+                if (lane < 2) {
+                    float *a = sm.u.p2.acc + cl * 4 + 2 * lane;
+                    kahan(a[0], a[1], lane == 0 ? qv[0] : qv[1]);
+                }
+            }
+            __syncthreads();
+        }
+        for (int k = threadIdx.x; k < nc * 2; k += kT) {
+            const int cl = k >> 1, comp = k & 1;
+            I.qpart[((size_t)grp * I.C + cs + cl) * 2 + comp] =
+                (double)sm.u.p2.acc[cl * 4 + 2 * comp] - (double)sm.u.p2.acc[cl * 4 + 2 * comp + 1];
+        }
         __syncthreads();
     }
 }
@@ -778,133 +982,6 @@ __global__ void k32_cell_macros(const F32Inst *__restrict__ insts, const int *__
 }
 
 // =============================================================================
-// P2: face values, flux, evolution, heat-flux partials
-// =============================================================================
-__global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
-                                                   int nitems, int cur) {
-    extern __shared__ float4 smem_raw[];
-    TileSmem &sm = *reinterpret_cast<TileSmem *>(smem_raw);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    init_barriers(sm);
-    unsigned uses[2] = {0u, 0u};
-    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const int2 item = items[it];
-        const F32Inst &I = insts[item.x];
-        if (step_stopped(I.status)) continue;
-        const int tile = item.y / I.ngroup, grp = item.y % I.ngroup;
-        const int cs = I.tile_cstart[tile], nc = I.tile_ncell[tile];
-        const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
-        const int ch0 = grp * cpg, ch1 = min(I.chunks, ch0 + cpg);
-        if (ch0 >= ch1) continue;
-        const float2 *__restrict__ S = I.S[cur];
-        float2 *__restrict__ Sn = I.S[cur ^ 1];
-        const int NVp = I.NVp;
-        const float hdt = (float)I.hdt;
-        const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
-        const int grad_on = I.gradient;
-        const float *__restrict__ xi32x = I.xi32x;
-        const float *__restrict__ xi32y = I.xi32y;
-        const float *__restrict__ w32 = I.w32;
-        const float2 *__restrict__ bnd_out = I.bnd_out;
-        stage_common(I, tile, sm);
-        // tile cells: evolution constants and their faces
-        const int j0 = I.cf_ptr[cs];
-        for (int c = threadIdx.x; c < nc; c += kT) sm.u.p2.ck[c] = I.ck[cs + c];
-        for (int c = threadIdx.x; c <= nc; c += kT) sm.u.p2.cf_off[c] = I.cf_ptr[cs + c] - j0;
-        const int ncf = I.cf_ptr[cs + nc] - j0;
-        for (int e = threadIdx.x; e < ncf; e += kT) {
-            const int j = j0 + e;
-            const int f = I.cf_face[j];
-            // owner test: the cell whose face list holds entry j
-            int lo = 0, hi = nc;
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (I.cf_ptr[cs + mid] <= j) lo = mid;
-                else hi = mid;
-            }
-            const bool own = I.fown[f] == cs + lo;
-            CellFace x;
-            x.n = I.fn32[f];
-            x.fdo = I.fdo[f];
-            x.fdn = I.fdn[f];
-            x.area_s = own ? I.farea[f] : -I.farea[f];
-            x.bnd = I.fbnd[f];
-            x.face = f;
-            x.oslot = I.cf_oslot[j];
-            x.own = own ? 1 : 0;
-            x.pad = 0;
-            if (x.bnd < 0) x.fk = I.fk[f];
-            sm.u.p2.cf[e] = x;
-        }
-        for (int k = threadIdx.x; k < nc * 4; k += kT) sm.u.p2.acc[k] = 0.f;
-        __syncthreads();
-        if (warp == 0) issue_chunk(S, NVp, ch0, 0, sm);
-        for (int ch = ch0; ch < ch1; ++ch) {
-            const int buf = (ch - ch0) & 1;
-            if (warp == 0 && ch + 1 < ch1) issue_chunk(S, NVp, ch + 1, buf ^ 1, sm);
-            if (!wait_or_bail(sm, buf, uses[buf] & 1u, I.status)) return;
-            ++uses[buf];
-            gradients(sm, buf, grad_on, sm);
-            __syncthreads();
-            const int p = ch * 32 + lane;
-            const float xx = xi32x[p], xy = xi32y[p], w = w32[p];
-            const float hx = hdt * xx, hy = hdt * xy;
-            for (int cl = warp; cl < nc; cl += F32_WARPS) {
-                float fg = 0.f, fh = 0.f;
-                for (int e = sm.u.p2.cf_off[cl]; e < sm.u.p2.cf_off[cl + 1]; ++e) {
-                    const CellFace &x = sm.u.p2.cf[e];
-                    const float d = fmaf(x.n.x, xx, x.n.y * xy);
-                    const float knA = d * x.area_s;
-                    float2 gf;
-                    if (x.bnd >= 0) {
-                        gf = bnd_out[(size_t)x.bnd * NVp + p];
-                    } else {
-                        const int os = x.own ? cl : x.oslot, ns = x.own ? x.oslot : cl;
-                        const int cls = classify(I, x.face, p, d, xx, xy);
-                        const float2 gb = face_bar(sm, buf, cls, os, ns, x.fdo, x.fdn, hx, hy);
-                        const FaceK &k = x.fk;
-                        const float2 gs = shakhov(xx - k.ux, xy - k.uy, k.A, k.bl, k.qx, k.qy, k.sg, k.sh, k.iRT, k.hm,
-                                                  k3, twoK);
-                        gf = make_float2(fmaf(k.oCs, gb.x, k.Cs * gs.x), fmaf(k.oCs, gb.y, k.Cs * gs.y));
-                    }
-                    fg = fmaf(knA, gf.x, fg);
-                    fh = fmaf(knA, gf.y, fh);
-                }
-                const CellK &k = sm.u.p2.ck[cl];
-                const float2 old = sm.phi[buf][cl * 32 + lane];
-                // state n (cdugks_shakhov.cpp:673-680)
-                const float2 sn = shakhov(xx - k.unx, xy - k.uny, k.An, k.bln, k.qnx, k.qny, k.sgn, k.shn, k.iRTn,
-                                          k.hmn, k3, twoK);
-                const float gn = fmaf(k.cm, sn.x - old.x, old.x);
-                const float hn = fmaf(k.cm, sn.y - old.y, old.y);
-                // state n+1 with q at n (:682-687)
-                const float cx = xx - k.ux, cy = xy - k.uy;
-                const float2 s1 = shakhov(cx, cy, k.A, k.bl, k.qnx, k.qny, k.sg, k.sh, k.iRT, k.hm, k3, twoK);
-                // evolution (:689-690)
-                const float g = k.C * (gn + k.hdt_tau * s1.x + k.hdt_taun * (sn.x - gn) - k.dt_v * fg);
-                const float h = k.C * (hn + k.hdt_tau * s1.y + k.hdt_taun * (sn.y - hn) - k.dt_v * fh);
-                Sn[(size_t)(cs + cl) * NVp + p] = make_float2(fmaf(k.Cs, s1.x - g, g), fmaf(k.Cs, s1.y - h, h));
-                // heat-flux partial (:692)
-                const float hw = 0.5f * w * fmaf(fmaf(cx, cx, cy * cy), g, h);
-                float qv[2] = {hw * cx, hw * cy};
-                warp_sum(qv);
-                if (lane < 2) {
-                    float *a = sm.u.p2.acc + cl * 4 + 2 * lane;
-                    kahan(a[0], a[1], lane == 0 ? qv[0] : qv[1]);
-                }
-            }
-            __syncthreads();
-        }
-        for (int k = threadIdx.x; k < nc * 2; k += kT) {
-            const int cl = k >> 1, comp = k & 1;
-            I.qpart[((size_t)grp * I.C + cs + cl) * 2 + comp] =
-                (double)sm.u.p2.acc[cl * 4 + 2 * comp] - (double)sm.u.p2.acc[cl * 4 + 2 * comp + 1];
-        }
-        __syncthreads();
-    }
-}
-
-// =============================================================================
 // QR: heat flux from the partials; mask repair; end of step
 // =============================================================================
 __global__ void k32_heat_flux(const F32Inst *__restrict__ insts, const int *__restrict__ coff, int ninst, int total,
@@ -1042,9 +1119,11 @@ int grid_of(int total, int per_block, int cap) {
 
 int fp32_configure(int device) {
     (void)device;
-    if (cudaFuncSetAttribute(k32_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem) != cudaSuccess)
-        return -1;
-    if (cudaFuncSetAttribute(k32_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem) != cudaSuccess)
+    const int a1 = (int)tile_smem<1>(), a2 = (int)tile_smem<2>();
+    if (cudaFuncSetAttribute(k32_moments<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, a1) != cudaSuccess ||
+        cudaFuncSetAttribute(k32_update<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, a1) != cudaSuccess ||
+        cudaFuncSetAttribute(k32_moments<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, a2) != cudaSuccess ||
+        cudaFuncSetAttribute(k32_update<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, a2) != cudaSuccess)
         return -1;
     return 0;
 }
@@ -1055,12 +1134,27 @@ const char *const kFp32Phases[] = {"k32_moments", "k32_face_macros", "k32_face_e
 int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev) {
     const int sms = s.num_sms;
     const int cap = sms * 32;
-    const int tile_grid = s.nitems < sms ? s.nitems : sms;  // one persistent CTA per SM
+    // one persistent CTA per SM; items of vpl == 2 instances, then those of vpl == 1, each its own launch
+    const int n2 = s.nitems_vpl2, n1 = s.nitems - s.nitems_vpl2;
+    const int grid2 = n2 < sms ? n2 : sms, grid1 = n1 < sms ? n1 : sms;
+    int n = 0;
+    auto tiles = [&](bool update) {
+        if (n2 > 0) {
+            if (update) k32_update<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2, s.cur);
+            else k32_moments<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2, s.cur);
+            ++n;
+        }
+        if (n1 > 0) {
+            if (update) k32_update<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1, s.cur);
+            else k32_moments<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1, s.cur);
+            ++n;
+        }
+    };
     auto mark = [&](int k) {
         if (ev) cudaEventRecord(ev[k], stream);
     };
     mark(0);
-    k32_moments<<<tile_grid, kT, kTileSmem, stream>>>(s.d_inst, s.d_items, s.nitems, s.cur);
+    tiles(false);
     mark(1);
     k32_face_macros<<<grid_of(s.total_faces, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
                                                                           s.total_faces);
@@ -1068,7 +1162,7 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     k32_face_eqflux<<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
                                                                         s.total_faces);
     mark(3);
-    int n = 3;
+    n += 2;
     if (s.total_bnd > 0) {
         k32_boundary<<<grid_of(s.total_bnd, 1, cap), 256, 0, stream>>>(s.d_inst, s.d_bnd_items, s.ninst, s.total_bnd);
         ++n;
@@ -1077,14 +1171,14 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     k32_cell_macros<<<grid_of(s.total_cells, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_cell_items, s.ninst,
                                                                           s.total_cells);
     mark(5);
-    k32_update<<<tile_grid, kT, kTileSmem, stream>>>(s.d_inst, s.d_items, s.nitems, s.cur);
+    tiles(true);
     mark(6);
     k32_heat_flux<<<grid_of(s.total_cells, 256, cap), 256, 0, stream>>>(s.d_inst, s.d_cell_items, s.ninst,
                                                                         s.total_cells, 1);
     k32_mask_repair<<<32, 256, 0, stream>>>(s.d_inst, s.ninst, s.cur ^ 1);
     k32_end_step<<<(s.ninst + 63) / 64, 64, 0, stream>>>(s.d_inst, s.ninst);
     mark(7);
-    n += 6;
+    n += 4;
     if (launches) *launches += n;
     s.cur ^= 1;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;

@@ -14,14 +14,14 @@
 namespace meso {
 
 // Kernel limits (the tile planner shrinks tiles until every tile fits).
-constexpr int F32_LANES = 32;       // velocities per chunk (one per lane)
 constexpr int F32_WARPS = 16;       // warps per CTA of the tile kernels
-constexpr int F32_MAX_SLOTS = 160;  // tile + two-ring halo cells
-constexpr int F32_MAX_GSLOTS = 112; // tile + one-ring halo cells (gradients)
-constexpr int F32_MAX_GENT = 640;   // gradient stencil entries per tile
-constexpr int F32_MAX_OWNED = 144;  // faces owned by a tile
-constexpr int F32_MAX_CELLS = 64;   // cells per tile
-constexpr int F32_MAX_CF = 256;     // cell-face entries per tile (tile cells x faces per cell)
+constexpr int F32_MAX_VPL = 2;      // velocities per lane (a chunk is 32 x VPL velocities)
+constexpr int F32_MAX_SLOTS = 104;  // tile + two-ring halo cells
+constexpr int F32_MAX_GSLOTS = 72;  // tile + one-ring halo cells (gradients)
+constexpr int F32_MAX_GENT = 432;   // gradient stencil entries per tile
+constexpr int F32_MAX_OWNED = 100;  // faces owned by a tile
+constexpr int F32_MAX_CELLS = 40;   // cells per tile
+constexpr int F32_MAX_CF = 160;     // cell-face entries per tile (tile cells x faces per cell)
 constexpr int F32_NMOM = 11;        // raw face moments about the reference velocity (2-D)
 
 // Face equilibrium scalars for FP32 evaluation of g_S, h_S at a face.
@@ -44,7 +44,8 @@ struct CellK {
 };
 
 struct F32Inst {
-    int C, F, NV, NVp, nb, ntile, ngroup, chunks;  // chunks = NVp / 32
+    int C, F, NV, NVp, nb, ntile, ngroup, chunks;  // chunks = NVp / (32 vpl)
+    int vpl;                                       // velocities per lane: 1 or 2
     // physics
     double dt, hdt, R, Pr, mu0, vhs, T0, Kd, Cv, gamma;
     int gradient;
@@ -92,6 +93,7 @@ struct Fp32State {
     F32Inst *d_inst = nullptr;   // device copy of the instance array
     int2 *d_items = nullptr;     // (inst, tile * ngroup + group) work items
     int nitems = 0;
+    int nitems_vpl2 = 0;         // the first nitems_vpl2 items belong to instances with vpl == 2
     int *d_face_items = nullptr; // prefix sums of faces / cells / boundary faces over instances
     int *d_cell_items = nullptr;
     int *d_bnd_items = nullptr;
