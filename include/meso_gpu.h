@@ -285,6 +285,44 @@ int meso_phase_times(meso_ctx *ctx, int32_t nsteps, double *ms, int32_t max_phas
 /* Kernel name(s) of phase i of this context's step. */
 const char *meso_phase_name(meso_ctx *ctx, int32_t i);
 
+/* ---- allocation-free entry point --------------------------------------- */
+
+/* Largest ncell meso_shakhov_moments_noalloc accepts. */
+#define MESO_NOALLOC_MAX_CELLS 131072
+
+/*
+ * Macroscopic moments of a Shakhov state, for callers that cannot call
+ * cudaMalloc: a host framework that owns all device memory in its own pool
+ * and gives an operator only its input and output buffers, or a serving /
+ * real-time loop with a fixed memory budget that must not call cudaMalloc or
+ * cudaFree (both synchronize the device) between steps.  No counterpart in
+ * the reference; it evaluates the moment sums of initial() (cdugks_shakhov.cpp:
+ * 102-169) on the caller's buffers.
+ *
+ *   g, h   [ncell*nv] state, cell-major (velocity fastest), FP64
+ *   xi     [nv*3], w [nv]: discrete velocities and weights
+ *   u0     [ncell*3] velocity the heat flux is taken about (c = xi - u0)
+ *   R, K   gas constant and gas-k (Cv = (K + 3) R / 2)
+ *   rho [ncell], u [ncell*3], T [ncell], q [ncell*3]: outputs
+ *   stream a cudaStream_t (NULL: the default stream); the outputs are ready
+ *          when the stream reaches the call
+ * Every array is device (or managed) memory of the current device.
+ *
+ * Allocates nothing: no cudaMalloc, cudaFree or allocating library call.
+ * Its scratch is one fixed device array of 8 MiB + 64 KiB in this library,
+ * present on every GPU that loads the library until the process exits; hence
+ * ncell <= MESO_NOALLOC_MAX_CELLS, larger requests fail with
+ * MESO_ERR_CAPACITY.  The first call on a device looks up that array's
+ * device address (and loads the library's device code there if it is not
+ * loaded yet); make that first call before any stream capture.  Every call
+ * on a device shares the array: calls that may overlap on the GPU (other
+ * streams without ordering, other host threads) race and give wrong results;
+ * order them on one stream or synchronize between them.
+ */
+int meso_shakhov_moments_noalloc(const double *g, const double *h, int32_t ncell, int32_t nv, int32_t dim,
+                                 const double *xi, const double *w, const double *u0, double R, double K,
+                                 double *rho, double *u, double *T, double *q, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,7 +29,8 @@ HOST_SRCS = ["host/mesh.cpp", "host/config.cpp", "host/case.cpp", "host/renumber
              "host/tiles.cpp", "host/fp32_host.cpp", "capi.cpp"]
 # (source, extra nvcc flags)
 CUDA_SRCS = [("kernels/plain_fp64.cu", ["-fmad=false"]),
-             ("kernels/fp32_step.cu", [])]
+             ("kernels/fp32_step.cu", []),
+             ("kernels/moments_noalloc.cu", ["-fmad=false"])]
 
 LIB = os.path.join(LIBDIR, "libmeso_gpu.so")
 ORACLE_LIB = os.path.join(ORACLE, "lib", "libmeso_oracle.so")

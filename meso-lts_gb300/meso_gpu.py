@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(_HERE, "lib", "libmeso_gpu.so")
 OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_NAN, ERR_TIMEOUT, ERR_IO, ERR_UNSUPPORTED, ERR_CAPACITY = range(9)
 SOLVER_DUGKS, SOLVER_CDUGKS, SOLVER_CDUGKS_SHAKHOV = 0, 1, 2
 FP64, FP32 = 0, 1
+NOALLOC_MAX_CELLS = 131072  # MESO_NOALLOC_MAX_CELLS
 BC = dict(fluid_interior=0, farfield_inlet=1, pressure_inlet=2, freestream_inlet=3, farfield_outlet=4,
           pressure_outlet=5, wall=6, slip_wall=7, symmetry=8)
 
@@ -104,6 +105,10 @@ _SIGS = {
     "meso_last_step_launches": (C.c_int64, [C.c_void_p]),
     "meso_phase_times": (C.c_int, [C.c_void_p, C.c_int32, _dp, C.c_int32, _ip]),
     "meso_phase_name": (C.c_char_p, [C.c_void_p, C.c_int32]),
+    # device pointers are passed as integers (c_void_p)
+    "meso_shakhov_moments_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                               C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p,
+                                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 EXPORTED = tuple(_SIGS)
