@@ -9,6 +9,8 @@
 
 namespace meso_host {
 
+constexpr double kPI_HOST = 3.14159265358979323846;
+
 bool plan_fp32(const meso_mesh_desc &m, int tile_cells, Renumbering &rn, TilePlan &plan) {
     for (int T = std::min(tile_cells, meso::F32_MAX_CELLS); T >= 4; T = T * 7 / 8) {
         std::vector<int> sizes;
@@ -65,6 +67,8 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
     I.Kd = (double)p.K;
     I.Cv = (p.K + 3.0) * p.R * 0.5;
     I.gamma = (p.K + 5.0) / (p.K + 3.0);
+    I.rho0 = p.rho0 > 0.0 ? p.rho0 : 1.0;
+    I.hm0 = (p.K + 1.0) * p.R * p.T0;
     I.gradient = p.gradient_switch;
     // renumbered face geometry and boundary index
     std::vector<int> fown(F), fnei(F), fbnd(F, -1), bface, fmark(F);
@@ -101,6 +105,26 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         xx[q] = (float)xx64[q];
         xy[q] = (float)xy64[q];
         w[q] = (float)w64[q];
+    }
+    // reference Maxwellian g0 = rho0 / (2 pi R T0) exp(-|xi|^2 / (2 R T0)) and its discrete moments
+    std::vector<double> g064(NVp, 0.0);
+    std::vector<float> g032(NVp, 0.f);
+    {
+        const double over = 0.5 / (p.R * p.T0);
+        double sum[10] = {0}, cmp[10] = {0};
+        for (int q = 0; q < NV; ++q) {
+            const double x = xx64[q], y = xy64[q];
+            g064[q] = I.rho0 * over / kPI_HOST * std::exp(-(x * x + y * y) * over);
+            g032[q] = (float)g064[q];
+            const double wg = w64[q] * g064[q];
+            const double mono[10] = {1.0, x, y, x * x, x * y, y * y, x * x * x, x * x * y, x * y * y, y * y * y};
+            for (int k = 0; k < 10; ++k) {  // compensated (Neumaier) sums
+                const double v = wg * mono[k], t = sum[k] + v;
+                cmp[k] += std::fabs(sum[k]) >= std::fabs(v) ? (sum[k] - t) + v : (v - t) + sum[k];
+                sum[k] = t;
+            }
+        }
+        for (int k = 0; k < 10; ++k) I.gmom[k] = sum[k] + cmp[k];
     }
     std::vector<int> sym(3 * (size_t)NV, 0);
     if (d->sym)
@@ -145,6 +169,8 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.xi64x = up(A, xx64, s);
         I.xi64y = up(A, xy64, s);
         I.w64 = up(A, w64, s);
+        I.g0_32 = up(A, g032, s);
+        I.g0_64 = up(A, g064, s);
         I.sym = up(A, sym, s);
         const size_t cv = (size_t)C * NVp;
         I.S[0] = A.alloc<float2>(cv);
@@ -157,6 +183,7 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.fsum = A.alloc<double>((size_t)F * 4);
         I.bnd_in = A.alloc<float2>((size_t)std::max(I.nb, 1) * NVp);
         I.bnd_out = A.alloc<float2>((size_t)std::max(I.nb, 1) * NVp);
+        I.bnd_g0 = A.alloc<double>(2 * (size_t)std::max(I.nb, 1));
         I.ck = A.alloc<meso::CellK>(C);
         I.qpart = A.alloc<double>((size_t)I.ngroup * C * 2);
         I.rho = A.alloc<double>(C);
@@ -189,6 +216,7 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
     std::vector<meso::F32Inst> one(1, I);
     c->fs.cur = 0;
     if (build_fp32_launch(one, c->num_sms, c->fs, c->fs_owned)) return fail(MESO_ERR_OOM, "launch state allocation failed");
+    if (meso::fp32_prepare(c->fs, s)) return fail(MESO_ERR_CUDA, "FP32 set-up kernel failed");
     cudaStreamSynchronize(s);
     return MESO_OK;
 }

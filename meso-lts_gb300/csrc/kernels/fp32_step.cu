@@ -65,16 +65,92 @@ __device__ __forceinline__ int classify(const F32Inst &I, int f, int p, float d3
     return d >= kVSMALL ? 0 : (d < -kVSMALL ? 1 : 2);
 }
 
-// Shakhov g and h at one velocity (2-D) from precomputed scalars (cdugks_shakhov.cpp:185-211).
-__device__ __forceinline__ float2 shakhov(float cx, float cy, float A, float bl, float qx, float qy, float sg,
-                                          float sh, float iRT, float hm, float k3, float twoK) {
+// exp(x) - 1 in FP32 with a small relative error near 0: the Taylor series of
+// exp through x^8 for |x| < 1/2 (truncation below 1.1e-8 relative), exp(x) - 1
+// from ex2.approx beyond (|exp(x) - 1| > 0.39 there).  Branch-free.
+__device__ __forceinline__ float expm1_dev(float x) {
+    float p = fmaf(x, 1.f / 40320.f, 1.f / 5040.f);
+    p = fmaf(x, p, 1.f / 720.f);
+    p = fmaf(x, p, 1.f / 120.f);
+    p = fmaf(x, p, 1.f / 24.f);
+    p = fmaf(x, p, 1.f / 6.f);
+    p = fmaf(x, p, 0.5f);
+    p = fmaf(x, p, 1.f);
+    const float series = x * p;
+    const float direct = fast_ex2(x * (float)kLOG2E) - 1.f;
+    return fabsf(x) < 0.5f ? series : direct;
+}
+
+// Deviation of the Shakhov g, h (2-D, cdugks_shakhov.cpp:185-211) at one velocity
+// from the reference pair (g0, hm0 g0):
+//   g_M = g0 + dg_M,  dg_M = g0 expm1(E)
+//   g_S - g0 = dg_M + g_M (1 - Pr) (c.q) / (5 p R T) (c^2 / RT - 4)
+//   h_S - h0 = hm dg_M + dhm g0 + g_M (1 - Pr) (c.q) / (5 p) ((c^2 / RT - 2)(K + 1) - 2K)
+__device__ __forceinline__ float2 dshakhov(const EqP &e, float xx, float xy, float g0, float k3, float twoK) {
+    const float xi2 = fmaf(xx, xx, xy * xy);
+    const float E = fmaf(e.ea, xi2, fmaf(e.ebx, xx, fmaf(e.eby, xy, e.ec)));
+    const float dgm = g0 * expm1_dev(E);
+    const float gm = g0 + dgm;
+    const float cx = xx - e.ux, cy = xy - e.uy;
     const float cc = fmaf(cx, cx, cy * cy);
-    const float cq = fmaf(cx, qx, cy * qy);
-    const float gm = A * fast_ex2(-cc * bl);
-    const float t = cc * iRT;
-    const float g = gm * fmaf(sg * cq, t - 4.0f, 1.0f);
-    const float h = gm * fmaf(sh * cq, fmaf(t - 2.0f, k3, -twoK), hm);
-    return make_float2(g, h);
+    const float cq = fmaf(cx, e.qx, cy * e.qy);
+    const float t = cc * e.iRT;
+    const float dg = fmaf(gm * (e.sg * cq), t - 4.0f, dgm);
+    const float dh = fmaf(gm * (e.sh * cq), fmaf(t - 2.0f, k3, -twoK), fmaf(e.hm, dgm, e.dhm * g0));
+    return make_float2(dg, dh);
+}
+
+// EqP of (rho, u, T, q), from FP64 macros.
+__device__ __forceinline__ EqP make_eqp(const F32Inst &I, double rho, double ux, double uy, double T, double qx,
+                                        double qy) {
+    const double RT = I.R * T, p = rho * RT, iRT = 1.0 / RT;
+    EqP e;
+    e.ux = (float)ux;
+    e.uy = (float)uy;
+    e.qx = (float)qx;
+    e.qy = (float)qy;
+    e.ea = (float)(0.5 / (I.R * I.T0) - 0.5 * iRT);
+    e.ebx = (float)(ux * iRT);
+    e.eby = (float)(uy * iRT);
+    e.ec = (float)(log(rho * I.T0 / (I.rho0 * T)) - 0.5 * (ux * ux + uy * uy) * iRT);
+    e.sg = (float)((1.0 - I.Pr) / (5.0 * p * RT));
+    e.sh = (float)((1.0 - I.Pr) / (5.0 * p));
+    e.iRT = (float)iRT;
+    e.hm = (float)((I.Kd + 1.0) * RT);
+    e.dhm = (float)((I.Kd + 1.0) * I.R * (T - I.T0));
+    return e;
+}
+
+// The 11 raw moments of the reference pair about velocity (a, b), from the discrete
+// moments of g0 (same order as the moments k32_moments accumulates).
+__device__ __forceinline__ void g0_raw_moments(const F32Inst &I, double a, double b, double (&M)[F32_NMOM]) {
+    const double *G = I.gmom;  // 1, x, y, xx, xy, yy, xxx, xxy, xyy, yyy
+    const double g1 = G[0], gx = G[1], gy = G[2], gxx = G[3], gxy = G[4], gyy = G[5];
+    const double gxxx = G[6], gxxy = G[7], gxyy = G[8], gyyy = G[9];
+    M[0] = g1;
+    M[1] = gx - a * g1;
+    M[2] = gy - b * g1;
+    M[3] = gxx - 2.0 * a * gx + a * a * g1;
+    M[4] = gxy - a * gy - b * gx + a * b * g1;
+    M[5] = gyy - 2.0 * b * gy + b * b * g1;
+    const double cxxx = gxxx - 3.0 * a * gxx + 3.0 * a * a * gx - a * a * a * g1;
+    const double cxyy = gxyy - a * gyy - 2.0 * b * gxy + 2.0 * a * b * gy + b * b * gx - a * b * b * g1;
+    const double cyyy = gyyy - 3.0 * b * gyy + 3.0 * b * b * gy - b * b * b * g1;
+    const double cxxy = gxxy - b * gxx - 2.0 * a * gxy + 2.0 * a * b * gx + a * a * gy - a * a * b * g1;
+    M[6] = cxxx + cxyy;
+    M[7] = cyyy + cxxy;
+    M[8] = I.hm0 * g1;
+    M[9] = I.hm0 * (gx - a * g1);
+    M[10] = I.hm0 * (gy - b * g1);
+}
+
+// Fluxes of the reference pair along n (mass, momentum x, y, energy), full velocity set.
+__device__ __forceinline__ void g0_fluxes(const F32Inst &I, double nx, double ny, double (&o)[4]) {
+    const double *G = I.gmom;
+    o[0] = nx * G[1] + ny * G[2];
+    o[1] = nx * G[3] + ny * G[4];
+    o[2] = nx * G[4] + ny * G[5];
+    o[3] = nx * (G[6] + G[8]) + ny * (G[7] + G[9]) + I.hm0 * (nx * G[1] + ny * G[2]);
 }
 
 __device__ __forceinline__ void kahan(float &s, float &c, float v) {
@@ -467,6 +543,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         const float *__restrict__ xi32x = I.xi32x;
         const float *__restrict__ xi32y = I.xi32y;
         const float *__restrict__ w32 = I.w32;
+        const float *__restrict__ g0_32 = I.g0_32;
         const float2 *__restrict__ bnd_out = I.bnd_out;
         stage_common(I, tile, sm);
         const int j0 = I.cf_ptr[cs];
@@ -507,7 +584,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
             else ++use0;
             gradients(sm, buf, grad_on);
             __syncthreads();
-            float xx[VPL], xy[VPL], w[VPL], hx[VPL], hy[VPL];
+            float xx[VPL], xy[VPL], w[VPL], hx[VPL], hy[VPL], g0[VPL];
             int p[VPL];
 #pragma unroll
             for (int v = 0; v < VPL; ++v) {
@@ -515,6 +592,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                 xx[v] = xi32x[p[v]];
                 xy[v] = xi32y[p[v]];
                 w[v] = w32[p[v]];
+                g0[v] = g0_32[p[v]];
                 hx[v] = hdt * xx[v];
                 hy[v] = hdt * xy[v];
             }
@@ -545,8 +623,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                             const float d = fmaf(n.x, xx[v], n.y * xy[v]);
                             const int cls = classify(I, x.face, p[v], d, xx[v], xy[v]);
                             const float2 gb = face_bar(sm, buf, v, cls, os, ns, fdo, fdn, hx[v], hy[v]);
-                            const float2 gs = shakhov(xx[v] - k.ux, xy[v] - k.uy, k.A, k.bl, k.qx, k.qy, k.sg, k.sh,
-                                                      k.iRT, k.hm, k3, twoK);
+                            const float2 gs = dshakhov(k.e, xx[v], xy[v], g0[v], k3, twoK);
                             const float knA = d * area_s;
                             fg[v] = fmaf(knA, fmaf(k.oCs, gb.x, k.Cs * gs.x), fg[v]);
                             fh[v] = fmaf(knA, fmaf(k.oCs, gb.y, k.Cs * gs.y), fh[v]);
@@ -559,13 +636,12 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                 for (int v = 0; v < VPL; ++v) {
                     const float2 old = sm.phi[buf][cl * SEG + v * 32 + lane];
                     // state n (cdugks_shakhov.cpp:673-680)
-                    const float2 sn = shakhov(xx[v] - k.unx, xy[v] - k.uny, k.An, k.bln, k.qnx, k.qny, k.sgn, k.shn,
-                                              k.iRTn, k.hmn, k3, twoK);
+                    const float2 sn = dshakhov(k.en, xx[v], xy[v], g0[v], k3, twoK);
                     const float gn = fmaf(k.cm, sn.x - old.x, old.x);
                     const float hn = fmaf(k.cm, sn.y - old.y, old.y);
                     // state n+1 with q at n (:682-687)
-                    const float cx = xx[v] - k.ux, cy = xy[v] - k.uy;
-                    const float2 s1 = shakhov(cx, cy, k.A, k.bl, k.qnx, k.qny, k.sg, k.sh, k.iRT, k.hm, k3, twoK);
+                    const float cx = xx[v] - k.e1.ux, cy = xy[v] - k.e1.uy;
+                    const float2 s1 = dshakhov(k.e1, xx[v], xy[v], g0[v], k3, twoK);
                     // evolution (:689-690)
                     const float g = k.C * (gn + k.hdt_tau * s1.x + k.hdt_taun * (sn.x - gn) - k.dt_v * fg[v]);
                     const float h = k.C * (hn + k.hdt_tau * s1.y + k.hdt_taun * (sn.y - hn) - k.dt_v * fh[v]);
@@ -610,6 +686,11 @@ __global__ void k32_face_macros(const F32Inst *__restrict__ insts, const int *__
         }
         const float2 uo = I.u32[I.fown[f]], un = I.u32[I.fnei[f]];
         const double u0x = (double)(0.5f * (uo.x + un.x)), u0y = (double)(0.5f * (uo.y + un.y));
+        {  // the reference pair's part of the moments, exactly in FP64
+            double M0[F32_NMOM];
+            g0_raw_moments(I, u0x, u0y, M0);
+            for (int k = 0; k < F32_NMOM; ++k) M[k] += M0[k];
+        }
         const double rho = M[0];
         const double dx = M[1] / rho, dy = M[2] / rho;
         const double ux = u0x + dx, uy = u0y + dy;
@@ -632,20 +713,11 @@ __global__ void k32_face_macros(const F32Inst *__restrict__ insts, const int *__
         fm[5] = qy;
         fm[6] = Cs;
         fm[7] = tau;
-        const double RT = I.R * T, p = rho * RT;
         FaceK k;
-        k.ux = (float)ux;
-        k.uy = (float)uy;
-        k.qx = (float)qx;
-        k.qy = (float)qy;
-        k.A = (float)(rho / (2.0 * kPI * RT));
-        k.bl = (float)(kLOG2E / (2.0 * RT));
-        k.sg = (float)((1.0 - I.Pr) / (5.0 * p * RT));
-        k.sh = (float)((1.0 - I.Pr) / (5.0 * p));
-        k.iRT = (float)(1.0 / RT);
-        k.hm = (float)((I.Kd + 1.0) * RT);
+        k.e = make_eqp(I, rho, ux, uy, T, qx, qy);
         k.Cs = (float)Cs;
         k.oCs = (float)(1.0 - Cs);
+        k.pad0 = 0.f;
         I.fk[f] = k;
         // moment fluxes of the reconstructed values along n0 (per unit area)
         const double2 n = I.fn64[f];
@@ -681,7 +753,7 @@ __global__ void __launch_bounds__(256) k32_face_eqflux(const F32Inst *__restrict
         float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
         for (int p = lane; p < I.NVp; p += 32) {
             const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
-            const float2 gs = shakhov(xx - k.ux, xy - k.uy, k.A, k.bl, k.qx, k.qy, k.sg, k.sh, k.iRT, k.hm, k3, twoK);
+            const float2 gs = dshakhov(k.e, xx, xy, I.g0_32[p], k3, twoK);
             const float wkn = w * fmaf(n.x, xx, n.y * xy);
             const float a = wkn * gs.x;
             kahan(s[0], c[0], a);
@@ -692,11 +764,13 @@ __global__ void __launch_bounds__(256) k32_face_eqflux(const F32Inst *__restrict
         float v[4] = {s[0] - c[0], s[1] - c[1], s[2] - c[2], s[3] - c[3]};
         warp_sum(v);
         if (lane == 0) {
+            double g0f[4];
+            g0_fluxes(I, I.fn64[f].x, I.fn64[f].y, g0f);
             double *o = I.fsum + (size_t)f * 4;
-            o[0] = v[0];
-            o[1] = v[1];
-            o[2] = v[2];
-            o[3] = v[3];
+            o[0] = g0f[0] + v[0];
+            o[1] = g0f[1] + v[1];
+            o[2] = g0f[2] + v[2];
+            o[3] = g0f[3] + v[3];
         }
     }
 }
@@ -737,10 +811,10 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
         float2 *bin = I.bnd_in + (size_t)b * I.NVp;
         float2 *bout = I.bnd_out + (size_t)b * I.NVp;
         const float2 n = I.fn32[f];
-        // blend with the face equilibrium (cdugks_shakhov.cpp:350-361)
+        const double2 n64 = I.fn64[f];
+        // blend with the face equilibrium (cdugks_shakhov.cpp:350-361), deviations from (g0, h0)
         for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
-            const float xx = I.xi32x[p], xy = I.xi32y[p];
-            const float2 gs = shakhov(xx - k.ux, xy - k.uy, k.A, k.bl, k.qx, k.qy, k.sg, k.sh, k.iRT, k.hm, k3, twoK);
+            const float2 gs = dshakhov(k.e, I.xi32x[p], I.xi32y[p], I.g0_32[p], k3, twoK);
             const float2 gb = bin[p];
             bin[p] = make_float2(fmaf(k.oCs, gb.x, k.Cs * gs.x), fmaf(k.oCs, gb.y, k.Cs * gs.y));
         }
@@ -751,7 +825,7 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
         int mode = 0;  // 0 keep, 1 Maxwell incoming, 2 wall, 3 slip wall, 4 symmetry
         if (type == MESO_BC_PRESSURE_INLET) {
             const double T_m = I.T[nb], umx = I.u[3 * nb], umy = I.u[3 * nb + 1];
-            const double nx = -(double)I.fn64[f].x, ny = -(double)I.fn64[f].y;
+            const double nx = -n64.x, ny = -n64.y;
             const double s = umx * nx + umy * ny;
             uux = nx * s;
             uuy = ny * s;
@@ -773,7 +847,7 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
         } else if (type == MESO_BC_PRESSURE_OUTLET) {
             const double umx = I.u[3 * nb], umy = I.u[3 * nb + 1], T_m = I.T[nb];
             rr = solve_pressure(mk.pressure, I.R, T_m, umx, umy, I.gamma) / (I.R * T_m);
-            const double nx = (double)I.fn64[f].x, ny = (double)I.fn64[f].y;  // nv_e = -nv = n0
+            const double nx = n64.x, ny = n64.y;  // nv_e = -nv = n0
             const double s = umx * nx + umy * ny;
             uux = nx * s;
             uuy = ny * s;
@@ -794,27 +868,27 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
         }
         double rho_w = 0.0, den_w = 0.0;
         if (mode == 2 || mode == 3) {
+            // diffuse-wall density balance (cdugks_shakhov.cpp:468-497): outgoing mass of the
+            // blended face values over the incoming mass of a unit-density wall Maxwellian
+            // g0 (1 + expm1(E_w)); the g0 parts are the precomputed half-range sums
             double T_w = 0.0;
             if (mk.temperature_type == MESO_PATCH_ZERO_GRADIENT) T_w = I.T[nb];
             else if (mk.temperature_type == MESO_PATCH_FIXED_VALUE) T_w = mk.temperature;
-            const double RTw = I.R * T_w;
-            const float Aw = (float)(1.0 / (2.0 * kPI * RTw)), blw = (float)(kLOG2E / (2.0 * RTw));
-            const float uwx = (float)mk.velocity[0], uwy = (float)mk.velocity[1];
+            const EqP ew = make_eqp(I, 1.0, mk.velocity[0], mk.velocity[1], T_w, 0.0, 0.0);
             float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
             for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
                 const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
                 const float d = fmaf(n.x, xx, n.y * xy);
                 const int cls = classify(I, f, p, d, xx, xy);
-                const float kn = -d;
-                if (cls == 1) {  // kn >= VSMALL
-                    const float cx = xx - uwx, cy = xy - uwy;
-                    kahan(s1, c1, kn * w * Aw * fast_ex2(-fmaf(cx, cx, cy * cy) * blw));
+                if (cls == 1) {  // kn = -d >= VSMALL
+                    const float E = fmaf(ew.ea, fmaf(xx, xx, xy * xy), fmaf(ew.ebx, xx, fmaf(ew.eby, xy, ew.ec)));
+                    kahan(s1, c1, -d * w * I.g0_32[p] * expm1_dev(E));
                 } else {
-                    kahan(s0, c0, -kn * w * bin[p].x);
+                    kahan(s0, c0, d * w * bin[p].x);
                 }
             }
-            const double num = block_sum((double)s0 - (double)c0, sh);
-            const double den = block_sum((double)s1 - (double)c1, sh);
+            const double num = I.bnd_g0[2 * b] + block_sum((double)s0 - (double)c0, sh);
+            const double den = I.bnd_g0[2 * b + 1] + block_sum((double)s1 - (double)c1, sh);
             rho_w = num / den;
             den_w = den;
             rr = rho_w;
@@ -822,15 +896,14 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
             uux = mk.velocity[0];
             uuy = mk.velocity[1];
         }
-        const double RT = I.R * TT;
-        const float A = (float)(rr / (2.0 * kPI * RT)), bl = (float)(kLOG2E / (2.0 * RT)), hm = (float)((I.Kd + 1.0) * RT);
-        const float ux = (float)uux, uy = (float)uuy;
+        // incoming Maxwellian (rr, uu, TT) as a deviation from (g0, h0)
+        const EqP ein = make_eqp(I, rr > 0.0 ? rr : 1.0, uux, uuy, TT > 0.0 ? TT : I.T0, 0.0, 0.0);
         const int dir = mk.direction;
         const float au = (float)mk.alpha_u, aT = (float)mk.alpha_T;
         // The balance and the incoming set use the same temperature only for a fixedValue wall
         // (a zeroGradient wall balances with T_cell but sets with the patch scalar, :473-479 vs :533).
         const bool exact_mass = mode == 2 && mk.temperature_type == MESO_PATCH_FIXED_VALUE;
-        float s[4] = {0.f, 0.f, 0.f, 0.f}, cc4[4] = {0.f, 0.f, 0.f, 0.f};
+        float sm4[4] = {0.f, 0.f, 0.f, 0.f}, cm4[4] = {0.f, 0.f, 0.f, 0.f};
         for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
             const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
             const float d = fmaf(n.x, xx, n.y * xy);
@@ -843,9 +916,7 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
                     if (cls == 1) v = r;
                     else if (cls == 2) v = make_float2(0.5f * (v.x + r.x), 0.5f * (v.y + r.y));
                 } else if (cls != 0) {
-                    const float cx = xx - ux, cy = xy - uy;
-                    const float gm = A * fast_ex2(-fmaf(cx, cx, cy * cy) * bl);
-                    float2 inc = make_float2(gm, hm * gm);
+                    float2 inc = dshakhov(ein, xx, xy, I.g0_32[p], k3, twoK);
                     if (mode == 3) {
                         const float2 r = bin[I.sym[3 * p + dir]];
                         inc = make_float2((1.f - au) * inc.x + au * r.x, (1.f - aT) * inc.y + aT * r.y);
@@ -858,22 +929,57 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
                 }
             }
             bout[p] = v;
-            // moment fluxes of the final face values along n0
+            // moment fluxes of the deviations along n0 (the g0 parts are added in FP64 below)
             const float wkn = w * d;
             const float a = wkn * v.x;
-            // diffuse wall: the incoming mass flux is rho_w * den exactly (added below in FP64), so
-            // the face carries no net mass in FP32 storage either (cdugks_shakhov.cpp:468-497)
-            if (!(exact_mass && cls == 1)) kahan(s[0], cc4[0], a);
-            kahan(s[1], cc4[1], a * xx);
-            kahan(s[2], cc4[2], a * xy);
-            kahan(s[3], cc4[3], wkn * fmaf(fmaf(xx, xx, xy * xy), v.x, v.y));
+            // diffuse wall: the incoming mass flux is rho_w * den exactly (added below), so the face
+            // carries no net mass in FP32 storage either (cdugks_shakhov.cpp:468-497)
+            if (!(exact_mass && cls == 1)) kahan(sm4[0], cm4[0], a);
+            kahan(sm4[1], cm4[1], a * xx);
+            kahan(sm4[2], cm4[2], a * xy);
+            kahan(sm4[3], cm4[3], wkn * fmaf(fmaf(xx, xx, xy * xy), v.x, v.y));
         }
         double tot[4];
-        for (int q = 0; q < 4; ++q) tot[q] = block_sum((double)s[q] - (double)cc4[q], sh);
-        if (exact_mass) tot[0] -= rho_w * den_w;
+        for (int q = 0; q < 4; ++q) tot[q] = block_sum((double)sm4[q] - (double)cm4[q], sh);
+        double g0f[4];
+        g0_fluxes(I, n64.x, n64.y, g0f);
+        // exact-mass wall: the g0 mass over the non-incoming set is the balance's numerator part
+        tot[0] += exact_mass ? I.bnd_g0[2 * b] - rho_w * den_w : g0f[0];
+        for (int q = 1; q < 4; ++q) tot[q] += g0f[q];
         if (threadIdx.x == 0) {
             double *o = I.fsum + (size_t)f * 4;
             for (int q = 0; q < 4; ++q) o[q] = tot[q];
+        }
+        __syncthreads();
+    }
+}
+
+// Half-range sums of the reference Maxwellian over each boundary face (static: geometry and
+// velocity set only): [2b] = sum over non-incoming xi of (xi.n0) w g0, [2b+1] = sum over
+// incoming xi of (xi.n_in) w g0, with the step's classification.  One block per face, FP64.
+__global__ void __launch_bounds__(256) k32_bnd_setup(const F32Inst *__restrict__ insts, const int *__restrict__ boff,
+                                                    int ninst, int total) {
+    __shared__ double sh[8];
+    for (int g = blockIdx.x; g < total; g += gridDim.x) {
+        const int i = find_inst(boff, ninst, g);
+        const F32Inst &I = insts[i];
+        const int b = g - boff[i];
+        const int f = I.bface[b];
+        const float2 n = I.fn32[f];
+        const double2 n64 = I.fn64[f];
+        double s0 = 0.0, s1 = 0.0;
+        for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
+            const float xx = I.xi32x[p], xy = I.xi32y[p];
+            const int cls = classify(I, f, p, fmaf(n.x, xx, n.y * xy), xx, xy);
+            const double d = n64.x * I.xi64x[p] + n64.y * I.xi64y[p];
+            const double t = d * I.w64[p] * I.g0_64[p];
+            if (cls == 1) s1 -= t;
+            else s0 += t;
+        }
+        const double a = block_sum(s0, sh), c = block_sum(s1, sh);
+        if (threadIdx.x == 0) {
+            I.bnd_g0[2 * b] = a;
+            I.bnd_g0[2 * b + 1] = c;
         }
         __syncthreads();
     }
@@ -940,25 +1046,8 @@ __global__ void k32_cell_macros(const F32Inst *__restrict__ insts, const int *__
         I.T[c] = T;
         I.u32[c] = make_float2((float)ux, (float)uy);
         CellK k;
-        const double RTn = I.R * T_n, pn = rho_n * RTn, RT = I.R * T, p = rho * RT;
-        k.unx = (float)unx;
-        k.uny = (float)uny;
-        k.qnx = (float)qnx;
-        k.qny = (float)qny;
-        k.An = (float)(rho_n / (2.0 * kPI * RTn));
-        k.bln = (float)(kLOG2E / (2.0 * RTn));
-        k.sgn = (float)((1.0 - I.Pr) / (5.0 * pn * RTn));
-        k.shn = (float)((1.0 - I.Pr) / (5.0 * pn));
-        k.iRTn = (float)(1.0 / RTn);
-        k.hmn = (float)((I.Kd + 1.0) * RTn);
-        k.ux = (float)ux;
-        k.uy = (float)uy;
-        k.A = (float)(rho / (2.0 * kPI * RT));
-        k.bl = (float)(kLOG2E / (2.0 * RT));
-        k.sg = (float)((1.0 - I.Pr) / (5.0 * p * RT));
-        k.sh = (float)((1.0 - I.Pr) / (5.0 * p));
-        k.iRT = (float)(1.0 / RT);
-        k.hm = (float)((I.Kd + 1.0) * RT);
+        k.en = make_eqp(I, rho_n, unx, uny, T_n, qnx, qny);
+        k.e1 = make_eqp(I, rho, ux, uy, T, qnx, qny);
         k.cm = (float)(I.hdt / (I.hdt - 2.0 * tau_n));
         k.C = (float)(tau / (tau + I.hdt));
         k.Cs = (float)(I.hdt / (2.0 * tau));
@@ -996,6 +1085,12 @@ __global__ void k32_heat_flux(const F32Inst *__restrict__ insts, const int *__re
             qx += I.qpart[((size_t)grp * I.C + c) * 2];
             qy += I.qpart[((size_t)grp * I.C + c) * 2 + 1];
         }
+        {  // the reference pair's part, 1/2 sum w c (c^2 g0 + h0) about the cell velocity
+            double M0[F32_NMOM];
+            g0_raw_moments(I, I.u[3 * c], I.u[3 * c + 1], M0);
+            qx += 0.5 * (M0[6] + M0[9]);
+            qy += 0.5 * (M0[7] + M0[10]);
+        }
         I.q[3 * c] = qx;
         I.q[3 * c + 1] = qy;
         I.q[3 * c + 2] = 0.0;
@@ -1023,14 +1118,17 @@ __global__ void k32_mask_repair(const F32Inst *__restrict__ insts, int ninst, in
                 sqy += wi * I.q[3 * nb + 1];
             }
             const double rho = sr / sw, T = sT / sw, ux = sux / sw, uy = suy / sw, qx = sqx / sw, qy = sqy / sw;
-            const double RT = I.R * T, p = rho * RT;
-            const float A = (float)(rho / (2.0 * kPI * RT)), bl = (float)(kLOG2E / (2.0 * RT));
-            const float sg = (float)((1.0 - I.Pr) / (5.0 * p * RT)), sh = (float)((1.0 - I.Pr) / (5.0 * p));
-            const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
-            for (int pp = threadIdx.x; pp < I.NVp; pp += blockDim.x)
-                I.S[nxt][(size_t)c * I.NVp + pp] =
-                    shakhov(I.xi32x[pp] - (float)ux, I.xi32y[pp] - (float)uy, A, bl, (float)qx, (float)qy, sg, sh,
-                            (float)(1.0 / RT), (float)((I.Kd + 1.0) * RT), k3, twoK);
+            const double RT = I.R * T, p = rho * RT, over = 0.5 / RT;
+            for (int pp = threadIdx.x; pp < I.NVp; pp += blockDim.x) {
+                const double cx = I.xi64x[pp] - ux, cy = I.xi64y[pp] - uy, cc = cx * cx + cy * cy;
+                const double cq = cx * qx + cy * qy;
+                const double gm = rho * over / kPI * exp(-cc * over);
+                const double gg = (1.0 - I.Pr) * (cq / (5.0 * p * RT)) * (cc / RT - 4.0) * gm + gm;
+                const double hh = (1.0 - I.Pr) * (cq / (5.0 * p)) * ((cc / RT - 2.0) * (I.Kd + 1.0) - 2.0 * I.Kd) * gm +
+                                  (I.Kd + 1.0) * RT * gm;
+                const double g0 = I.g0_64[pp];
+                I.S[nxt][(size_t)c * I.NVp + pp] = make_float2((float)(gg - g0), (float)(hh - I.hm0 * g0));
+            }
             if (threadIdx.x == 0) {
                 I.rho[c] = rho;
                 I.T[c] = T;
@@ -1082,7 +1180,8 @@ __global__ void k32_init(const F32Inst *__restrict__ insts, const int *__restric
                 hh = (1.0 - I.Pr) * (cq / (5.0 * p)) * ((cc / RT - 2.0) * (I.Kd + 1.0) - 2.0 * I.Kd) * gm +
                      (I.Kd + 1.0) * RT * gm;
             }
-            I.S[cur][(size_t)c * I.NVp + pp] = make_float2((float)gg, (float)hh);
+            const double g0 = I.g0_64[pp];
+            I.S[cur][(size_t)c * I.NVp + pp] = make_float2((float)(gg - g0), (float)(hh - I.hm0 * g0));
             v[0] += w * gg;
             v[1] += w * gg * xx;
             v[2] += w * gg * xy;
@@ -1181,6 +1280,13 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     n += 4;
     if (launches) *launches += n;
     s.cur ^= 1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int fp32_prepare(const Fp32State &s, cudaStream_t stream) {
+    if (s.total_bnd > 0)
+        k32_bnd_setup<<<grid_of(s.total_bnd, 1, s.num_sms * 32), 256, 0, stream>>>(s.d_inst, s.d_bnd_items, s.ninst,
+                                                                                 s.total_bnd);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -24,22 +24,32 @@ constexpr int F32_MAX_CELLS = 40;   // cells per tile
 constexpr int F32_MAX_CF = 160;     // cell-face entries per tile (tile cells x faces per cell)
 constexpr int F32_NMOM = 11;        // raw face moments about the reference velocity (2-D)
 
-// Face equilibrium scalars for FP32 evaluation of g_S, h_S at a face.
-struct FaceK {
+// Scalars of one Shakhov equilibrium (rho, u, T, q) for FP32 evaluation of its
+// deviation from the instance's reference Maxwellian g0 (see F32Inst::g0_32):
+//   g_M / g0 = exp(E),  E = ea |xi|^2 + ebx xi_x + eby xi_y + ec,
+//   ea = 1/(2 R T0) - 1/(2 R T),  eb = u / (R T),  ec = ln(rho T0 / (rho0 T)) - |u|^2 / (2 R T),
+// so that E, and with it g_M - g0 = g0 expm1(E), carries the rounding of the
+// deviation only.
+struct EqP {
     float ux, uy, qx, qy;
-    float A;    // rho / (2 pi R T)
-    float bl;   // log2(e) / (2 R T)
+    float ea, ebx, eby, ec;
     float sg;   // (1 - Pr) / (5 p R T)
     float sh;   // (1 - Pr) / (5 p)
     float iRT;  // 1 / (R T)
     float hm;   // (K + 3 - D) R T
-    float Cs, oCs;
+    float dhm;  // (K + 3 - D) R (T - T0)
 };
 
-// Per-cell evolution constants (states n and n+1).
+// Face equilibrium and blend weights.
+struct FaceK {
+    EqP e;
+    float Cs, oCs, pad0;
+};
+
+// Per-cell evolution constants: equilibria at states n and n+1 (the latter with q at n,
+// cdugks_shakhov.cpp:684) and the evolution coefficients.
 struct CellK {
-    float unx, uny, qnx, qny, An, bln, sgn, shn, iRTn, hmn;
-    float ux, uy, A, bl, sg, sh, iRT, hm;
+    EqP en, e1;
     float cm, C, Cs, hdt_tau, hdt_taun, dt_v;
 };
 
@@ -47,7 +57,10 @@ struct F32Inst {
     int C, F, NV, NVp, nb, ntile, ngroup, chunks;  // chunks = NVp / (32 vpl)
     int vpl;                                       // velocities per lane: 1 or 2
     // physics
-    double dt, hdt, R, Pr, mu0, vhs, T0, Kd, Cv, gamma;
+    double dt, hdt, R, Pr, mu0, vhs, T0, Kd, Cv, gamma, rho0;
+    // reference Maxwellian g0 (rho0, u = 0, T0) and h0 = hm0 g0: the state holds g - g0, h - h0
+    double hm0;
+    double gmom[10];  // sum w g0 xi^a over the velocity set: 1, x, y, xx, xy, yy, xxx, xxy, xyy, yyy
     int gradient;
     // tile plan
     const int *tile_cstart, *tile_ncell, *tile_slot_ptr, *slot_cell, *tile_gslots, *tile_gsp_off, *gs_ptr;
@@ -68,9 +81,11 @@ struct F32Inst {
     // velocities (padded to NVp with zero weight)
     const float *xi32x, *xi32y, *w32;
     const double *xi64x, *xi64y, *w64;
+    const float *g0_32;    // [NVp] reference Maxwellian (0 on padding)
+    const double *g0_64;
     const int *sym;
     // state and work buffers
-    float2 *S[2];          // [C][NVp] (g, h) ping-pong
+    float2 *S[2];          // [C][NVp] (g - g0, h - h0) ping-pong
     double *fpart;         // [ngroup][F][11] raw face-moment partials
     float2 *u32;           // [C] cell velocity (FP32) = reference velocity of the face moments
     FaceK *fk;             // [F]
@@ -78,6 +93,7 @@ struct F32Inst {
     double *fgbar;         // [F][4] fluxes of the reconstructed values (mass, mom x, mom y, energy) per unit area along n0
     double *fsum;          // [F][4] same for the face equilibrium (interior) or the final boundary values
     float2 *bnd_in, *bnd_out;  // [nb][NVp]
+    double *bnd_g0;            // [nb][2] half-range sums of g0 (fp32_prepare)
     CellK *ck;             // [C]
     double *qpart;         // [ngroup][C][2]
     double *rho, *u, *T, *q;   // [C], [3C], [C], [3C]
@@ -107,6 +123,8 @@ constexpr int F32_NPHASE = 7;
 extern const char *const kFp32Phases[F32_NPHASE];
 // One step of every instance; ev (may be null) receives F32_NPHASE + 1 events around the phases.
 int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev = nullptr);
+// Once per instance set-up, after the instances are on the device.
+int fp32_prepare(const Fp32State &s, cudaStream_t stream);
 int fp32_init(const Fp32State &s, int mode, cudaStream_t stream);
 int fp32_finalize_q(const Fp32State &s, cudaStream_t stream);
 
