@@ -13,8 +13,9 @@
  *     No C++ exception crosses this boundary.
  *   - All arrays are caller-owned host memory, indexed in the ORIGINAL order
  *     of the .neu file (cells and faces as the reference numbers them); the
- *     library renumbers internally (reverse Cuthill-McKee cells, faces sorted
- *     by owner) and maps back on every read.
+ *     library renumbers internally (FP64: reverse Cuthill-McKee cells; FP32:
+ *     bisection tiles with a local RCM order; faces sorted by owner) and maps
+ *     back on every read.
  *   - One context per host thread at a time (contexts are not internally
  *     locked); each context owns one CUDA stream on the current device.
  *   - Vectors are xyz triples, 3 doubles per entry, also in 2D (z = 0).
@@ -47,7 +48,9 @@ extern "C" {
 
 /* ---- storage precision of the distribution functions -------------------- */
 #define MESO_FP64 0 /* plain form: f, face values and fluxes in FP64 (parity form)            */
-#define MESO_FP32 1 /* f stored and streamed in FP32; moments, equilibria, wall sums in FP64 */
+#define MESO_FP32 1 /* f stored and streamed in FP32 as the deviation from a reference Maxwellian;
+                       face / cell macros, the reference Maxwellian's moments and the wall
+                       balance in FP64 (2-D Shakhov without the limiter) */
 
 /* ---- boundary types: BoundaryType of include/solver/config.h:13-23 ------- */
 #define MESO_BC_FLUID_INTERIOR 0
@@ -154,7 +157,16 @@ typedef struct meso_params {
     double CFL;                  /* "CFL" (DUGKS) */
     double venkata_k;            /* "venkata-limiter-k" */
     double residual_limit;       /* "residual-limit" */
+    int32_t residual_fields;     /* fields the convergence test watches: 0 = all the reference watches
+                                    (cdugks_shakhov.cpp:747-756), else MESO_RES_* bits; no counterpart
+                                    in the reference (served solves converge on U) */
+    int32_t pad_;
 } meso_params;
+
+#define MESO_RES_RHO 1
+#define MESO_RES_T 2
+#define MESO_RES_U 4 /* every velocity component */
+#define MESO_RES_Q 8
 
 /* Step state, the reference's run_state / step / solution_time plus the monitor of cdugks_shakhov.cpp:697-719. */
 typedef struct meso_status {
@@ -284,6 +296,31 @@ int64_t meso_last_step_launches(meso_ctx *ctx);
 int meso_phase_times(meso_ctx *ctx, int32_t nsteps, double *ms, int32_t max_phases, int32_t *nphases);
 /* Kernel name(s) of phase i of this context's step. */
 const char *meso_phase_name(meso_ctx *ctx, int32_t i);
+
+/* ---- batched solves ----------------------------------------------------- */
+
+/*
+ * A batch steps many FP32 contexts (different meshes, velocity sets and
+ * parameters) with one set of launches per step, replayed as a CUDA graph.
+ * No counterpart in the reference, which runs one solve per process: each
+ * member keeps the reference's per-solve do_step bookkeeping (step,
+ * solution_time, residual every residual_interval of its own steps and the
+ * 10-check convergence counter, cdugks_shakhov.cpp:724-764); a member that
+ * converges or hits an unmasked NaN / T < 0 stops taking steps.  Members must be
+ * FP32 contexts on one device, initialised, and in no other batch; while in a
+ * batch they are stepped only by meso_batch_step (meso_step refuses them) and
+ * do not re-read their case files.  Results, status, output and snapshots are
+ * read per member with the meso_ctx functions.  Destroying a member removes it
+ * from its batch; destroying the batch leaves the members intact.
+ */
+int meso_batch_create(meso_ctx *const *ctxs, int32_t n, meso_batch **out);
+void meso_batch_destroy(meso_batch *batch);
+/* nsteps steps of every running member; *nrunning (may be NULL) receives the members still running. */
+int meso_batch_step(meso_batch *batch, int32_t nsteps, int32_t *nrunning);
+int32_t meso_batch_size(meso_batch *batch);
+/* Device time of the last meso_batch_step call (ms) and the kernel launches it issued. */
+double meso_batch_last_step_ms(meso_batch *batch);
+int64_t meso_batch_last_step_launches(meso_batch *batch);
 
 /* ---- allocation-free entry point --------------------------------------- */
 

@@ -388,20 +388,27 @@ int residual_check(meso_ctx *c) {
     double ru[3];
     residual_vector(c, c->u_res, u, ru);
     std::vector<double> list;
+    std::vector<int> field;  // MESO_RES_* of each entry
+    const int D = c->dim;
     if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV) {
         double rT = residual_scalar(c, c->T_res, T);
         double rq[3];
         residual_vector(c, c->q_res, q, rq);
-        if (c->dim == 2) list = {rr, rT, ru[0], ru[1], rq[0], rq[1]};
-        else list = {rr, rT, ru[0], ru[1], ru[2], rq[0], rq[1], rq[2]};
+        list = {rr, rT};
+        field = {MESO_RES_RHO, MESO_RES_T};
+        for (int k = 0; k < D; ++k) list.push_back(ru[k]), field.push_back(MESO_RES_U);
+        for (int k = 0; k < D; ++k) list.push_back(rq[k]), field.push_back(MESO_RES_Q);
     } else {
-        if (c->dim == 2) list = {rr, ru[0], ru[1]};
-        else list = {rr, ru[0], ru[1], ru[2]};
+        list = {rr};
+        field = {MESO_RES_RHO};
+        for (int k = 0; k < D; ++k) list.push_back(ru[k]), field.push_back(MESO_RES_U);
     }
     c->nres = (int)list.size();
     for (int i = 0; i < c->nres; ++i) c->last_res[i] = list[i];
+    const int watch = c->params.residual_fields;
     bool conv = true;
-    for (double v : list) conv = conv && (v <= c->params.residual_limit);
+    for (size_t i = 0; i < list.size(); ++i)
+        if (watch == 0 || (watch & field[i])) conv = conv && (list[i] <= c->params.residual_limit);
     if (conv) c->converge_state++;
     else c->converge_state = 0;
     if (c->converge_state >= 10) {
@@ -418,6 +425,28 @@ int launch_step(meso_ctx *c) {
     return MESO_OK;
 }
 
+// New step settings into the FP32 instance: time step, Prandtl number, viscosity law and the
+// gradient switch.  R, T0 and rho0 define the stored reference Maxwellian and stay fixed.
+int refresh_f32(meso_ctx *c) {
+    if (c->params.precision != MESO_FP32) return MESO_OK;
+    meso::F32Inst &I = c->f32;
+    const meso_params &p = c->params;
+    I.dt = p.dt;
+    I.hdt = p.dt * 0.5;
+    I.Pr = p.Pr;
+    I.mu0 = p.mu0;
+    I.vhs = p.vhs_index;
+    I.gradient = p.gradient_switch;
+    CUDA_TRY(cudaMemcpyAsync(c->fs.d_inst, &I, sizeof(I), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->f32_version++;
+    return MESO_OK;
+}
+
+bool fp32_fixed_changed(const meso_params &a, const meso_params &b) {
+    return a.R != b.R || a.T0 != b.T0 || a.rho0 != b.rho0 || a.K != b.K || a.limiter_switch != b.limiter_switch;
+}
+
 // Live reload of [settings] (cdugks_shakhov.cpp:762): the reference re-reads
 // the case file after every step; re-reading only when its mtime changed
 // gives the same settings without a file read per step.
@@ -430,8 +459,17 @@ void maybe_reload(meso_ctx *c) {
     try {
         c->kase->params.precision = c->params.precision;
         if (c->kase->reload_settings()) {
+            const meso_params prev = c->params;
             c->params = c->kase->params;
+            if (c->params.precision == MESO_FP32 && fp32_fixed_changed(prev, c->params)) {
+                c->params.R = prev.R;  // the FP32 form keeps its reference state
+                c->params.T0 = prev.T0;
+                c->params.rho0 = prev.rho0;
+                c->params.K = prev.K;
+                c->params.limiter_switch = prev.limiter_switch;
+            }
             derive_kparams(c->params, c->dim, c->ps.kp);
+            refresh_f32(c);
         }
     } catch (...) {
         // a half-written file keeps the current settings; the next change retries
@@ -508,13 +546,13 @@ int init_common(meso_ctx *c, const double *rho, const double *u, const double *T
     CUDA_TRY(cudaMemcpyAsync(c->ps.u, uu.data(), sizeof(double) * 3 * C, cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(cudaMemcpyAsync(c->ps.T, t.data(), sizeof(double) * C, cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(cudaMemcpyAsync(c->ps.q, qq.data(), sizeof(double) * 3 * C, cudaMemcpyHostToDevice, c->stream));
+    reset_status(c);  // step 0 first: the FP32 init writes S[step parity]
     if (c->params.precision == MESO_FP32) {
         if (meso::fp32_init(c->fs, mode, c->stream)) return fail(MESO_ERR_CUDA, "init kernel launch failed");
     } else if (meso::plain_init(c->ps, mode, c->stream)) {
         return fail(MESO_ERR_CUDA, "init kernel launch failed");
     }
     CUDA_TRY(cudaStreamSynchronize(c->stream));
-    reset_status(c);
     c->step = 0;
     c->solution_time = 0.0;
     c->run_state = 1;
@@ -558,6 +596,11 @@ std::vector<double> read_vector_file(const std::string &f, int n) {
     } while (0)
 
 }  // namespace
+
+namespace meso_host {
+int ctx_read_status(meso_ctx *c) { return read_status(c); }
+int ctx_residual_check(meso_ctx *c) { return residual_check(c); }
+}  // namespace meso_host
 
 extern "C" {
 
@@ -673,6 +716,7 @@ int meso_ctx_create_from_case(const char *case_file, int32_t precision, meso_ctx
 void meso_ctx_destroy(meso_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
+    if (c->batch) meso_host::batch_forget(c->batch, c);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_fp32_launch(c->fs, c->fs_owned);
     c->arena.release();
@@ -724,6 +768,7 @@ int meso_step(meso_ctx *c, int32_t nsteps, int32_t *steps_done) {
     if (steps_done) *steps_done = 0;
     if (!c->initialized) return fail(MESO_ERR_INVALID, "meso_step before initial()");
     if (nsteps < 0) return fail(MESO_ERR_INVALID, "nsteps must be >= 0");
+    if (c->batch) return fail(MESO_ERR_INVALID, "this context is stepped by its batch (meso_batch_step)");
     const int start = c->step;
     std::vector<double> dts;
     dts.reserve(nsteps);
@@ -819,9 +864,11 @@ int meso_set_params(meso_ctx *c, const meso_params *p) {
         return fail(MESO_ERR_INVALID, "solver and precision are fixed for a context");
     std::string why;
     if (!valid_params(*p, why)) return fail(MESO_ERR_INVALID, why);
+    if (c->params.precision == MESO_FP32 && fp32_fixed_changed(c->params, *p))
+        return fail(MESO_ERR_UNSUPPORTED, "the FP32 form fixes R, T0, rho0, K and the limiter switch at creation");
     c->params = *p;
     derive_kparams(c->params, c->dim, c->ps.kp);
-    return MESO_OK;
+    return refresh_f32(c);
 }
 
 int meso_get_params(meso_ctx *c, meso_params *p) {
@@ -890,7 +937,9 @@ int meso_snapshot(meso_ctx *c, void *host, size_t bytes) {
         p += n * sizeof(double);
     };
     if (c->params.precision == MESO_FP32) {
-        cudaMemcpyAsync(p, c->f32.S[c->fs.cur], state_bytes(c), cudaMemcpyDeviceToHost, c->stream);
+        int rc = read_status(c);  // the current FP32 buffer is S[device step parity]
+        if (rc) return rc;
+        cudaMemcpyAsync(p, c->f32.S[c->h_status->step & 1], state_bytes(c), cudaMemcpyDeviceToHost, c->stream);
         p += state_bytes(c);
     } else {
         d2h(c->ps.f0, cv);
@@ -919,7 +968,9 @@ int meso_restore(meso_ctx *c, const void *host, size_t bytes) {
         p += n * sizeof(double);
     };
     if (c->params.precision == MESO_FP32) {
-        cudaMemcpyAsync(c->f32.S[c->fs.cur], p, state_bytes(c), cudaMemcpyHostToDevice, c->stream);
+        meso::DStatus ds;
+        std::memcpy(&ds, p + state_bytes(c) + sizeof(double) * 8 * (size_t)c->C, sizeof(ds));
+        cudaMemcpyAsync(c->f32.S[ds.step & 1], p, state_bytes(c), cudaMemcpyHostToDevice, c->stream);
         p += state_bytes(c);
     } else {
         h2d(c->ps.f0, cv);

@@ -40,6 +40,11 @@ int fail(int code, const std::string &msg);
 
 void derive_kparams(const meso_params &p, int dim, meso::KParams &k);
 
+// Context helpers shared with the batch and server front ends (capi.cpp).
+int ctx_read_status(meso_ctx *c);    // device status -> c->h_status (syncs the context's stream)
+int ctx_residual_check(meso_ctx *c); // residual + convergence counter of do_step
+void batch_forget(meso_batch *b, meso_ctx *c);  // batch.cpp
+
 }  // namespace meso_host
 
 struct meso_ctx {
@@ -79,4 +84,6 @@ struct meso_ctx {
     double last_ms = 0.0;
     int64_t last_launches = 0;
     std::time_t case_mtime = 0;
+    int f32_version = 0;  // bumped when the FP32 instance's settings change on the device
+    meso_batch *batch = nullptr;  // the batch this context is a member of, if any
 };

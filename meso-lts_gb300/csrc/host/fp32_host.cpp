@@ -214,7 +214,6 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
     c->ps.fm1 = I.fm1;
     c->ps.fm2 = I.fm2;
     std::vector<meso::F32Inst> one(1, I);
-    c->fs.cur = 0;
     if (build_fp32_launch(one, c->num_sms, c->fs, c->fs_owned)) return fail(MESO_ERR_OOM, "launch state allocation failed");
     if (meso::fp32_prepare(c->fs, s)) return fail(MESO_ERR_CUDA, "FP32 set-up kernel failed");
     cudaStreamSynchronize(s);

@@ -86,8 +86,8 @@ __device__ __forceinline__ float expm1_dev(float x) {
 //   g_M = g0 + dg_M,  dg_M = g0 expm1(E)
 //   g_S - g0 = dg_M + g_M (1 - Pr) (c.q) / (5 p R T) (c^2 / RT - 4)
 //   h_S - h0 = hm dg_M + dhm g0 + g_M (1 - Pr) (c.q) / (5 p) ((c^2 / RT - 2)(K + 1) - 2K)
-__device__ __forceinline__ float2 dshakhov(const EqP &e, float xx, float xy, float g0, float k3, float twoK) {
-    const float xi2 = fmaf(xx, xx, xy * xy);
+__device__ __forceinline__ float2 dshakhov(const EqP &e, float xx, float xy, float xi2, float g0, float k3,
+                                           float twoK) {
     const float E = fmaf(e.ea, xi2, fmaf(e.ebx, xx, fmaf(e.eby, xy, e.ec)));
     const float dgm = g0 * expm1_dev(E);
     const float gm = g0 + dgm;
@@ -410,7 +410,7 @@ template <int VPL> __device__ __forceinline__ void init_barriers(TileSmem<VPL> &
 // =============================================================================
 template <int VPL>
 __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
-                                                    int nitems, int cur) {
+                                                    int nitems) {
     constexpr int SEG = TileSmem<VPL>::SEG;
     extern __shared__ float4 smem_raw[];
     TileSmem<VPL> &sm = *reinterpret_cast<TileSmem<VPL> *>(smem_raw);
@@ -421,6 +421,7 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
         const int2 item = items[it];
         const F32Inst &I = insts[item.x];
         if (step_stopped(I.status)) continue;
+        const int cur = I.status->step & 1;  // S[step parity] holds the current state
         const int tile = item.y / I.ngroup, grp = item.y % I.ngroup;
         const int fs = I.tile_fstart[tile], nOF = I.tile_fstart[tile + 1] - fs;
         const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
@@ -518,7 +519,7 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
 // =============================================================================
 template <int VPL>
 __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
-                                                   int nitems, int cur) {
+                                                   int nitems) {
     constexpr int SEG = TileSmem<VPL>::SEG;
     extern __shared__ float4 smem_raw[];
     TileSmem<VPL> &sm = *reinterpret_cast<TileSmem<VPL> *>(smem_raw);
@@ -529,6 +530,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         const int2 item = items[it];
         const F32Inst &I = insts[item.x];
         if (step_stopped(I.status)) continue;
+        const int cur = I.status->step & 1;  // S[step parity] holds the current state
         const int tile = item.y / I.ngroup, grp = item.y % I.ngroup;
         const int cs = I.tile_cstart[tile], nc = I.tile_ncell[tile];
         const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
@@ -584,13 +586,14 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
             else ++use0;
             gradients(sm, buf, grad_on);
             __syncthreads();
-            float xx[VPL], xy[VPL], w[VPL], hx[VPL], hy[VPL], g0[VPL];
+            float xx[VPL], xy[VPL], w[VPL], hx[VPL], hy[VPL], g0[VPL], x2[VPL];
             int p[VPL];
 #pragma unroll
             for (int v = 0; v < VPL; ++v) {
                 p[v] = ch * SEG + v * 32 + lane;
                 xx[v] = xi32x[p[v]];
                 xy[v] = xi32y[p[v]];
+                x2[v] = fmaf(xx[v], xx[v], xy[v] * xy[v]);
                 w[v] = w32[p[v]];
                 g0[v] = g0_32[p[v]];
                 hx[v] = hdt * xx[v];
@@ -623,7 +626,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                             const float d = fmaf(n.x, xx[v], n.y * xy[v]);
                             const int cls = classify(I, x.face, p[v], d, xx[v], xy[v]);
                             const float2 gb = face_bar(sm, buf, v, cls, os, ns, fdo, fdn, hx[v], hy[v]);
-                            const float2 gs = dshakhov(k.e, xx[v], xy[v], g0[v], k3, twoK);
+                            const float2 gs = dshakhov(k.e, xx[v], xy[v], x2[v], g0[v], k3, twoK);
                             const float knA = d * area_s;
                             fg[v] = fmaf(knA, fmaf(k.oCs, gb.x, k.Cs * gs.x), fg[v]);
                             fh[v] = fmaf(knA, fmaf(k.oCs, gb.y, k.Cs * gs.y), fh[v]);
@@ -636,12 +639,12 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                 for (int v = 0; v < VPL; ++v) {
                     const float2 old = sm.phi[buf][cl * SEG + v * 32 + lane];
                     // state n (cdugks_shakhov.cpp:673-680)
-                    const float2 sn = dshakhov(k.en, xx[v], xy[v], g0[v], k3, twoK);
+                    const float2 sn = dshakhov(k.en, xx[v], xy[v], x2[v], g0[v], k3, twoK);
                     const float gn = fmaf(k.cm, sn.x - old.x, old.x);
                     const float hn = fmaf(k.cm, sn.y - old.y, old.y);
                     // state n+1 with q at n (:682-687)
                     const float cx = xx[v] - k.e1.ux, cy = xy[v] - k.e1.uy;
-                    const float2 s1 = dshakhov(k.e1, xx[v], xy[v], g0[v], k3, twoK);
+                    const float2 s1 = dshakhov(k.e1, xx[v], xy[v], x2[v], g0[v], k3, twoK);
                     // evolution (:689-690)
                     const float g = k.C * (gn + k.hdt_tau * s1.x + k.hdt_taun * (sn.x - gn) - k.dt_v * fg[v]);
                     const float h = k.C * (hn + k.hdt_tau * s1.y + k.hdt_taun * (sn.y - hn) - k.dt_v * fh[v]);
@@ -750,16 +753,23 @@ __global__ void __launch_bounds__(256) k32_face_eqflux(const F32Inst *__restrict
         const FaceK k = I.fk[f];
         const float2 n = I.fn32[f];
         const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
+        // plain FP32 sums over blocks of 8 velocities per lane, compensated across blocks
         float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int p = lane; p < I.NVp; p += 32) {
-            const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
-            const float2 gs = dshakhov(k.e, xx, xy, I.g0_32[p], k3, twoK);
-            const float wkn = w * fmaf(n.x, xx, n.y * xy);
-            const float a = wkn * gs.x;
-            kahan(s[0], c[0], a);
-            kahan(s[1], c[1], a * xx);
-            kahan(s[2], c[2], a * xy);
-            kahan(s[3], c[3], wkn * fmaf(fmaf(xx, xx, xy * xy), gs.x, gs.y));
+        for (int p0 = 0; p0 < I.NVp; p0 += 32 * 8) {
+            float b[4] = {0.f, 0.f, 0.f, 0.f};
+            const int pe = min(I.NVp, p0 + 32 * 8);
+            for (int p = p0 + lane; p < pe; p += 32) {
+                const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
+                const float x2 = fmaf(xx, xx, xy * xy);
+                const float2 gs = dshakhov(k.e, xx, xy, x2, I.g0_32[p], k3, twoK);
+                const float wkn = w * fmaf(n.x, xx, n.y * xy);
+                const float a = wkn * gs.x;
+                b[0] += a;
+                b[1] = fmaf(a, xx, b[1]);
+                b[2] = fmaf(a, xy, b[2]);
+                b[3] = fmaf(wkn, fmaf(x2, gs.x, gs.y), b[3]);
+            }
+            for (int q = 0; q < 4; ++q) kahan(s[q], c[q], b[q]);
         }
         float v[4] = {s[0] - c[0], s[1] - c[1], s[2] - c[2], s[3] - c[3]};
         warp_sum(v);
@@ -814,7 +824,8 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
         const double2 n64 = I.fn64[f];
         // blend with the face equilibrium (cdugks_shakhov.cpp:350-361), deviations from (g0, h0)
         for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
-            const float2 gs = dshakhov(k.e, I.xi32x[p], I.xi32y[p], I.g0_32[p], k3, twoK);
+            const float xx = I.xi32x[p], xy = I.xi32y[p];
+            const float2 gs = dshakhov(k.e, xx, xy, fmaf(xx, xx, xy * xy), I.g0_32[p], k3, twoK);
             const float2 gb = bin[p];
             bin[p] = make_float2(fmaf(k.oCs, gb.x, k.Cs * gs.x), fmaf(k.oCs, gb.y, k.Cs * gs.y));
         }
@@ -916,7 +927,7 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
                     if (cls == 1) v = r;
                     else if (cls == 2) v = make_float2(0.5f * (v.x + r.x), 0.5f * (v.y + r.y));
                 } else if (cls != 0) {
-                    float2 inc = dshakhov(ein, xx, xy, I.g0_32[p], k3, twoK);
+                    float2 inc = dshakhov(ein, xx, xy, fmaf(xx, xx, xy * xy), I.g0_32[p], k3, twoK);
                     if (mode == 3) {
                         const float2 r = bin[I.sym[3 * p + dir]];
                         inc = make_float2((1.f - au) * inc.x + au * r.x, (1.f - aT) * inc.y + aT * r.y);
@@ -1098,9 +1109,10 @@ __global__ void k32_heat_flux(const F32Inst *__restrict__ insts, const int *__re
 }
 
 // cell_value_interp (cdugks_shakhov.cpp:766-789) for queued masked cells, writing state n+1
-__global__ void k32_mask_repair(const F32Inst *__restrict__ insts, int ninst, int nxt) {
+__global__ void k32_mask_repair(const F32Inst *__restrict__ insts, int ninst) {
     for (int i = 0; i < ninst; ++i) {
         const F32Inst &I = insts[i];
+        const int nxt = (I.status->step & 1) ^ 1;  // before k32_end_step advances the step
         const int n = min(I.status->repair_count, I.C);
         for (int r = blockIdx.x; r < n; r += gridDim.x) {
             const int c = I.repair_list[r];
@@ -1144,7 +1156,7 @@ __global__ void k32_end_step(const F32Inst *__restrict__ insts, int ninst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ninst) return;
     DStatus *st = insts[i].status;
-    if (st->stop_step < st->step) return;
+    if (step_stopped(st)) return;
     st->repairs_total += st->repair_count;
     st->repair_count = 0;
     st->step += 1;
@@ -1155,13 +1167,14 @@ __global__ void k32_end_step(const F32Inst *__restrict__ insts, int ninst) {
 // (cdugks_shakhov.cpp:81-168).  One warp per cell.
 // =============================================================================
 __global__ void k32_init(const F32Inst *__restrict__ insts, const int *__restrict__ coff, int ninst, int total,
-                         int mode, int cur) {
+                         int mode) {
     const int lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
     for (int g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
         const int i = find_inst(coff, ninst, g);
         const F32Inst &I = insts[i];
         const int c = g - coff[i];
+        const int cur = I.status->step & 1;
         const double r = I.rho[c], ux = I.u[3 * c], uy = I.u[3 * c + 1], T = I.T[c];
         const double qx = I.q[3 * c], qy = I.q[3 * c + 1];
         const double RT = I.R * T, over = 0.5 / RT, p = r * RT;
@@ -1239,13 +1252,13 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     int n = 0;
     auto tiles = [&](bool update) {
         if (n2 > 0) {
-            if (update) k32_update<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2, s.cur);
-            else k32_moments<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2, s.cur);
+            if (update) k32_update<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
+            else k32_moments<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
             ++n;
         }
         if (n1 > 0) {
-            if (update) k32_update<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1, s.cur);
-            else k32_moments<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1, s.cur);
+            if (update) k32_update<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
+            else k32_moments<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
             ++n;
         }
     };
@@ -1274,12 +1287,11 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     mark(6);
     k32_heat_flux<<<grid_of(s.total_cells, 256, cap), 256, 0, stream>>>(s.d_inst, s.d_cell_items, s.ninst,
                                                                         s.total_cells, 1);
-    k32_mask_repair<<<32, 256, 0, stream>>>(s.d_inst, s.ninst, s.cur ^ 1);
+    k32_mask_repair<<<32, 256, 0, stream>>>(s.d_inst, s.ninst);
     k32_end_step<<<(s.ninst + 63) / 64, 64, 0, stream>>>(s.d_inst, s.ninst);
     mark(7);
     n += 4;
     if (launches) *launches += n;
-    s.cur ^= 1;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -1292,7 +1304,7 @@ int fp32_prepare(const Fp32State &s, cudaStream_t stream) {
 
 int fp32_init(const Fp32State &s, int mode, cudaStream_t stream) {
     k32_init<<<grid_of(s.total_cells, 8, s.num_sms * 32), 256, 0, stream>>>(s.d_inst, s.d_cell_items, s.ninst,
-                                                                           s.total_cells, mode, s.cur);
+                                                                           s.total_cells, mode);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -85,7 +85,7 @@ struct F32Inst {
     const double *g0_64;
     const int *sym;
     // state and work buffers
-    float2 *S[2];          // [C][NVp] (g - g0, h - h0) ping-pong
+    float2 *S[2];          // [C][NVp] (g - g0, h - h0) ping-pong; S[status->step & 1] is current
     double *fpart;         // [ngroup][F][11] raw face-moment partials
     float2 *u32;           // [C] cell velocity (FP32) = reference velocity of the face moments
     FaceK *fk;             // [F]
@@ -115,7 +115,6 @@ struct Fp32State {
     int *d_bnd_items = nullptr;
     int total_faces = 0, total_cells = 0, total_bnd = 0;
     int num_sms = 0;
-    int cur = 0;                 // which S buffer holds the current state
 };
 
 int fp32_configure(int device);

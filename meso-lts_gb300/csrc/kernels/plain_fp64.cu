@@ -869,7 +869,7 @@ __global__ void __launch_bounds__(kBlock) k_mask_repair(DMesh m, KParams k, DSta
 // End of step: count the step unless an earlier step stopped the run.
 __global__ void k_end_step(DStatus *st) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    if (st->stop_step < st->step) return;
+    if (step_stopped(st)) return;
     st->repairs_total += min(st->repair_count, INT_MAX);
     st->repair_count = 0;
     st->step += 1;

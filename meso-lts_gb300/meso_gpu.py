@@ -20,6 +20,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_NAN, ERR_TIMEOUT, ERR_IO, ERR_UNSUPPORTE
 SOLVER_DUGKS, SOLVER_CDUGKS, SOLVER_CDUGKS_SHAKHOV = 0, 1, 2
 FP64, FP32 = 0, 1
 NOALLOC_MAX_CELLS = 131072  # MESO_NOALLOC_MAX_CELLS
+RES_RHO, RES_T, RES_U, RES_Q = 1, 2, 4, 8  # MESO_RES_*
 BC = dict(fluid_interior=0, farfield_inlet=1, pressure_inlet=2, freestream_inlet=3, farfield_outlet=4,
           pressure_outlet=5, wall=6, slip_wall=7, symmetry=8)
 
@@ -54,7 +55,7 @@ class Params(C.Structure):
                 ("dt", C.c_double), ("R", C.c_double), ("T0", C.c_double), ("rho0", C.c_double),
                 ("L0", C.c_double), ("mu0", C.c_double), ("vhs_index", C.c_double), ("Pr", C.c_double),
                 ("Ma", C.c_double), ("Re", C.c_double), ("CFL", C.c_double), ("venkata_k", C.c_double),
-                ("residual_limit", C.c_double)]
+                ("residual_limit", C.c_double), ("residual_fields", C.c_int32), ("pad_", C.c_int32)]
 
 
 class Status(C.Structure):
@@ -105,6 +106,12 @@ _SIGS = {
     "meso_last_step_launches": (C.c_int64, [C.c_void_p]),
     "meso_phase_times": (C.c_int, [C.c_void_p, C.c_int32, _dp, C.c_int32, _ip]),
     "meso_phase_name": (C.c_char_p, [C.c_void_p, C.c_int32]),
+    "meso_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),
+    "meso_batch_destroy": (None, [C.c_void_p]),
+    "meso_batch_step": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "meso_batch_size": (C.c_int32, [C.c_void_p]),
+    "meso_batch_last_step_ms": (C.c_double, [C.c_void_p]),
+    "meso_batch_last_step_launches": (C.c_int64, [C.c_void_p]),
     # device pointers are passed as integers (c_void_p)
     "meso_shakhov_moments_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p,
@@ -316,6 +323,40 @@ class Solver:
     def close(self):
         if self._h:
             lib().meso_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """meso_batch: FP32 solvers stepped together (one set of launches per step)."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s.handle.value for s in self.solvers])
+        h = C.c_void_p()
+        _check(lib().meso_batch_create(arr, len(self.solvers), C.byref(h)))
+        self._h = h
+
+    def step(self, n: int = 1) -> int:
+        """n steps of every running member; returns the number still running."""
+        r = C.c_int32()
+        _check(lib().meso_batch_step(self._h, n, C.byref(r)))
+        return r.value
+
+    def last_step_ms(self) -> float:
+        return lib().meso_batch_last_step_ms(self._h)
+
+    def last_step_launches(self) -> int:
+        return lib().meso_batch_last_step_launches(self._h)
+
+    def close(self):
+        if self._h:
+            lib().meso_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):
