@@ -322,6 +322,38 @@ int32_t meso_batch_size(meso_batch *batch);
 double meso_batch_last_step_ms(meso_batch *batch);
 int64_t meso_batch_last_step_launches(meso_batch *batch);
 
+/* ---- served solves (continuous batching) -------------------------------- */
+
+/*
+ * A request server over one device.  Each request is a case file (FP32
+ * Shakhov); it is admitted when a member slot is free and the solve fits in
+ * the HBM budget and in the device's free memory, then stepped with every
+ * other admitted solve by one batch, with its state resident on the device.
+ * A solve finishes when it converges (residual settings from the case or the
+ * params given at submit), fails (unmasked NaN / T < 0) or reaches the case's
+ * max-step, as the reference's handle_solver loop ends a solve
+ * (src/meso/exec.cpp:141-165); its memory is then freed for pending requests.
+ * No counterpart in the reference, which runs one solve per process.
+ * One host thread drives a server.
+ */
+typedef struct meso_server meso_server;
+int meso_server_create(int64_t hbm_budget_bytes, int32_t max_members, meso_server **out);
+void meso_server_destroy(meso_server *server);
+/* Queue a solve; params (may be NULL) replaces the case file's settings.  *tag identifies it. */
+int meso_server_submit(meso_server *server, const char *case_file, const meso_params *params, int64_t *tag);
+/* Admit what fits, step the admitted solves nsteps together, retire the finished ones: their
+ * tags go to done_tags (capacity max_done), their count to *ndone. */
+int meso_server_poll(meso_server *server, int32_t nsteps, int64_t *done_tags, int32_t max_done, int32_t *ndone);
+int meso_server_counts(meso_server *server, int32_t *npending, int32_t *nrunning, int32_t *ndone);
+/* Result of a finished solve (original cell order; any pointer may be NULL); seconds[0] = submit to
+ * finish, seconds[1] = submit to admission (seconds may be NULL). */
+int meso_server_result(meso_server *server, int64_t tag, double *rho, double *u, double *T, double *q,
+                       meso_status *status, double *seconds);
+/* Drop a finished solve's stored result. */
+int meso_server_release(meso_server *server, int64_t tag);
+/* Device bytes held by the admitted solves. */
+int64_t meso_server_device_bytes(meso_server *server);
+
 /* ---- allocation-free entry point --------------------------------------- */
 
 /* Largest ncell meso_shakhov_moments_noalloc accepts. */

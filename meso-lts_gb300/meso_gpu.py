@@ -112,6 +112,14 @@ _SIGS = {
     "meso_batch_size": (C.c_int32, [C.c_void_p]),
     "meso_batch_last_step_ms": (C.c_double, [C.c_void_p]),
     "meso_batch_last_step_launches": (C.c_int64, [C.c_void_p]),
+    "meso_server_create": (C.c_int, [C.c_int64, C.c_int32, C.POINTER(C.c_void_p)]),
+    "meso_server_destroy": (None, [C.c_void_p]),
+    "meso_server_submit": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.POINTER(C.c_int64)]),
+    "meso_server_poll": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32)]),
+    "meso_server_counts": (C.c_int, [C.c_void_p, _ip, _ip, _ip]),
+    "meso_server_result": (C.c_int, [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, C.c_void_p, _dp]),
+    "meso_server_release": (C.c_int, [C.c_void_p, C.c_int64]),
+    "meso_server_device_bytes": (C.c_int64, [C.c_void_p]),
     # device pointers are passed as integers (c_void_p)
     "meso_shakhov_moments_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p,
@@ -357,6 +365,62 @@ class Batch:
     def close(self):
         if self._h:
             lib().meso_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """meso_server: served FP32 Shakhov solves with continuous batching."""
+
+    def __init__(self, hbm_budget_bytes: int, max_members: int = 64):
+        h = C.c_void_p()
+        _check(lib().meso_server_create(int(hbm_budget_bytes), int(max_members), C.byref(h)))
+        self._h = h
+        self.ncell = {}
+
+    def submit(self, case_path: str, params: Params | None = None) -> int:
+        t = C.c_int64()
+        _check(lib().meso_server_submit(self._h, os.fsencode(case_path),
+                                        C.byref(params) if params is not None else None, C.byref(t)))
+        c = Case(case_path)
+        self.ncell[t.value] = c.ncell
+        c.close()
+        return t.value
+
+    def poll(self, nsteps: int, max_done: int = 1024) -> list:
+        tags = (C.c_int64 * max_done)()
+        n = C.c_int32()
+        _check(lib().meso_server_poll(self._h, nsteps, tags, max_done, C.byref(n)))
+        return [tags[i] for i in range(n.value)]
+
+    def counts(self) -> tuple:
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        _check(lib().meso_server_counts(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def result(self, tag: int):
+        n = self.ncell[tag]
+        rho, u, T, q = np.zeros(n), np.zeros(3 * n), np.zeros(n), np.zeros(3 * n)
+        st = Status()
+        sec = np.zeros(2)
+        _check(lib().meso_server_result(self._h, tag, _ptr(rho), _ptr(u), _ptr(T), _ptr(q), C.byref(st), _ptr(sec)))
+        return (rho, u.reshape(n, 3), T, q.reshape(n, 3)), st, (float(sec[0]), float(sec[1]))
+
+    def release(self, tag: int):
+        _check(lib().meso_server_release(self._h, tag))
+        self.ncell.pop(tag, None)
+
+    def device_bytes(self) -> int:
+        return lib().meso_server_device_bytes(self._h)
+
+    def close(self):
+        if self._h:
+            lib().meso_server_destroy(self._h)
             self._h = None
 
     def __del__(self):
