@@ -197,7 +197,7 @@ def pinned(n: int):
     return np.frombuffer(buf, dtype=np.float64)
 
 
-def cpu_baseline(path: str, steps: int, threads: int) -> dict:
+def cpu_baseline(path: str, seconds: float, threads: int) -> dict:
     import meso_gpu as mg
     import meso_oracle as mo
 
@@ -205,9 +205,15 @@ def cpu_baseline(path: str, steps: int, threads: int) -> dict:
     rho, u, T, mask = case.initial_fields()
     o = mo.Oracle(case, threads, mask)
     o.init(rho, u, T, None, 0)
+    # one step to size the sample, then about `seconds` of steps (at most 30)
     t0 = time.perf_counter()
-    done, _ = o.step(steps)
-    secs = time.perf_counter() - t0
+    done, _ = o.step(1)
+    first = time.perf_counter() - t0
+    more = max(0, min(29, int(seconds / max(first, 1e-3)) - 1))
+    t1 = time.perf_counter()
+    d2, _ = o.step(more) if more else (0, 0)
+    done += d2
+    secs = first + (time.perf_counter() - t1)
     o.close()
     cx = case.ncell * case.nv
     return {"value": cx * done / secs, "unit": UNIT, "cores": threads, "kind": "port",
@@ -249,6 +255,116 @@ def run_reference(args, rank: int, dist: Dist) -> None:
         print(json.dumps(line), flush=True)
 
 
+def run_batched(tmp: str, steps: int = 20, warm: int = 3) -> dict:
+    """Config 4: 64 cavity instances (seeded draws of mesh side, Kn, velocity set, lid) in one batch."""
+    import cases
+    import meso_gpu as mg
+
+    insts = cases.config4_instances()
+    t0 = time.perf_counter()
+    members = []
+    for inst in insts:
+        path = cases.config4_case(os.path.join(tmp, f"b{inst['index']}"), inst, steps=1000000)
+        case = mg.Case(path)
+        rho, u, T, mask = case.initial_fields()
+        s = mg.Solver(case=case, precision=mg.FP32, mask=mask)
+        s.init_macros(rho, u, T, None, 0)
+        members.append((case, s))
+    setup_s = time.perf_counter() - t0
+    dev_bytes = sum(s.device_bytes() for _, s in members)
+    # the same instances stepped one at a time (device time per step, summed)
+    alone_ms = 0.0
+    for case, s in members:
+        s.step(1)
+        s.step(3)
+        alone_ms += s.last_step_ms() / 3
+    b = mg.Batch([s for _, s in members])
+    b.step(warm)
+    before = [s.status().step for _, s in members]
+    b.step(steps)
+    ms = b.last_step_ms()
+    launches = b.last_step_launches()
+    after = [s.status().step for _, s in members]
+    cx = sum(c.ncell * c.nv * (a - b0) for (c, _), a, b0 in zip(members, after, before))
+    stopped = sum(1 for _, s in members if s.status().run_state == 0)
+    cx_step = sum(c.ncell * c.nv for c, _ in members)
+    b.close()
+    for _, s in members:
+        s.close()
+    return {"workload": "64 Shakhov cavity instances, sides {32,48,64,96,128} quads, log10 Kn ~ U(-2,0), "
+                        "DVS {D2Q9, hGH 28x28, NC 101x101}, lid ~ U(0.05,0.15), seed 1, FP32 storage",
+            "value": cx / (ms * 1e-3), "unit": UNIT, "steps": steps, "ms_per_step": ms / steps,
+            "cell_xi_per_step": cx_step, "device_bytes": dev_bytes, "graph_launches_per_step": launches / steps,
+            "alone_ms_per_step_sum": alone_ms, "batch_over_alone": alone_ms / (ms / steps),
+            "members_stopped": stopped, "setup_seconds": setup_s}
+
+
+def run_served(tmp: str, count: int = 200, rate: float = 20.0, max_step: int = 8000, poll_steps: int = 100) -> dict:
+    """Config 5: a seeded Poisson stream of cavity solves, each run to convergence on U, served with
+    continuous batching; time-to-converged per request (submit to retirement)."""
+    import cases
+    import meso_gpu as mg
+
+    reqs = cases.config5_requests(count=count, rate=rate)
+    paths, params = [], []
+    for r in reqs:
+        p = cases.config5_case(os.path.join(tmp, f"s{r['index']}"), r, max_step)
+        prm = mg.Case(p).params
+        prm.residual_interval = 100
+        prm.residual_limit = 1e-6
+        prm.residual_fields = mg.RES_U | mg.RES_L2
+        paths.append(p)
+        params.append(prm)
+    rt = _cudart()
+    free_b, total_b = ctypes.c_size_t(), ctypes.c_size_t()
+    rt.cudaMemGetInfo(ctypes.byref(free_b), ctypes.byref(total_b))
+    srv = mg.Server(hbm_budget_bytes=int(free_b.value * 0.8), max_members=64)
+    done = {}
+    i = 0
+    t0 = time.perf_counter()
+    while len(done) < count:
+        now = time.perf_counter() - t0
+        while i < count and reqs[i]["arrival"] <= now:
+            srv.submit(paths[i], params[i])
+            i += 1
+        pend, run, _ = srv.counts()
+        if pend + run == 0:
+            time.sleep(max(0.0, min(0.01, reqs[i]["arrival"] - now)) if i < count else 0.0)
+            continue
+        for t in srv.poll(poll_steps):
+            _, st, sec = srv.result(t)
+            done[t] = (st.step, st.converged, st.run_state, sec[0], sec[1])
+            srv.release(t)
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = sorted(v[3] for v in done.values())
+    steps = [v[0] for v in done.values()]
+    conv = sum(v[1] for v in done.values())
+    # serial plain FP64: FP64 step time of each request class x the steps each solve took
+    cls_ms = {}
+    for r, p in zip(reqs, paths):
+        key = (r["side"], r["dvs"])
+        if key in cls_ms:
+            continue
+        case = mg.Case(p)
+        rho, u, T, mask = case.initial_fields()
+        s = mg.Solver(case=case, precision=mg.FP64, mask=mask)
+        s.init_macros(rho, u, T, None, 0)
+        s.step(2)
+        s.step(10)
+        cls_ms[key] = s.last_step_ms() / 10
+        s.close()
+    serial_s = sum(cls_ms[(r["side"], r["dvs"])] * 1e-3 * v[0] for r, v in zip(reqs, (done[k] for k in sorted(done))))
+    q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))]
+    return {"workload": f"{count} cavity solves, Poisson arrivals {rate}/s (seed 2), sides {{16,24,32}} quads, "
+                        "log10 Kn ~ U(-2,0), DVS {hGH 28x28, NC 21x21}, lid ~ U(0.05,0.15), FP32 storage, "
+                        f"run to L2-relative residual 1e-6 on U per 100 steps (max-step {max_step})",
+            "solves_per_s": count / wall, "wall_seconds": wall, "p50_s": q(0.50), "p99_s": q(0.99),
+            "converged": conv, "reached_max_step_or_failed": count - conv, "mean_steps": float(np.mean(steps)),
+            "serial_fp64_solves_per_s_est": count / serial_s if serial_s > 0 else None,
+            "serial_fp64_note": "FP64 step time of each request class x the steps each solve took, summed"}
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -256,6 +372,9 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--served-count", type=int, default=200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -367,7 +486,11 @@ def main() -> int:
             "gpu_launches": launches,
         }
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(path, 1, os.cpu_count() or 1)
+            line["cpu_baseline"] = cpu_baseline(path, 12.0, os.cpu_count() or 1)
+        if not args.no_batched:
+            line["batched"] = run_batched(tmp)
+        if not args.no_served:
+            line["served"] = run_served(tmp, count=args.served_count)
         if rank == 0:
             print(json.dumps(line), flush=True)
     dist.close()

@@ -167,6 +167,9 @@ typedef struct meso_params {
 #define MESO_RES_T 2
 #define MESO_RES_U 4 /* every velocity component */
 #define MESO_RES_Q 8
+#define MESO_RES_L2 16 /* measure volume-weighted L2-relative change ||new - old|| / ||old|| per component
+                          instead of the reference's mean of |new - old| / |old| (field.cpp:223-249),
+                          which divides by values near zero (velocity at a vortex centre) */
 
 /* Step state, the reference's run_state / step / solution_time plus the monitor of cdugks_shakhov.cpp:697-719. */
 typedef struct meso_status {

@@ -515,8 +515,35 @@ def config4_instances(seed: int = 1, count: int = 64) -> list[dict]:
 
 def config4_case(d: str, inst: dict, steps: int = 500, precision: str = "fp32") -> str:
     nv1d = {"d2q9": 3, "hgh": 28, "nc": 101}[inst["dvs"]]
+    # CFL 0.5 (the reference's shipped Kn 0.075 case runs at 0.66): at 0.8 the scheme is unstable on
+    # some of these cavities over a few hundred steps
     return shakhov_cavity(d, "quad", inst["side"], inst["dvs"], nv1d, inst["kn"], inst["lid"], steps,
-                          name=f"inst{inst['index']}", precision=precision)
+                          name=f"inst{inst['index']}", precision=precision, cfl=0.5)
+
+
+def config5_requests(seed: int = 2, count: int = 200, rate: float = 20.0,
+                     sides=(16, 24, 32), dvs_kinds=("hgh", "nc")) -> list[dict]:
+    """Served stream: Poisson arrivals (mean `rate` per second) of cavity solves drawn like config 4
+    (log10 Kn ~ U(-2,0), lid ~ U(.05,.15), DVS kind uniform) on the given mesh sides.  The velocity
+    sets are hGH 28x28 and NC 21x21: the reference scheme is unstable on the coarser hGH and D2Q9
+    sets above Kn ~ 0.1, and a request that blows up never converges."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(count):
+        t += float(rng.exponential(1.0 / rate))
+        side = int(rng.choice(list(sides)))
+        kn = float(10.0 ** rng.uniform(-2.0, 0.0))
+        dvs = dvs_kinds[int(rng.integers(0, len(dvs_kinds)))]
+        lid = float(rng.uniform(0.05, 0.15))
+        out.append(dict(index=i, arrival=t, side=side, kn=kn, dvs=dvs, lid=lid))
+    return out
+
+
+def config5_case(d: str, req: dict, max_step: int = 4000) -> str:
+    nv1d = {"d2q9": 3, "hgh": 28, "nc": 21}[req["dvs"]]
+    return shakhov_cavity(d, "quad", req["side"], req["dvs"], nv1d, req["kn"], req["lid"], max_step,
+                          name=f"req{req['index']}", precision="fp32", cfl=0.5)
 
 
 def shakhov_channel(d: str, kind: str = "pressure", nx: int = 10, ny: int = 6, dvs: str = "hgh", nv1d: int = 8,

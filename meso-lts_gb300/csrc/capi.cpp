@@ -379,11 +379,50 @@ void residual_vector(const meso_ctx *c, std::vector<double> &old, const std::vec
     out[2] = rz;
 }
 
+// Volume-weighted L2-relative change ||new - old|| / ||old|| of component k of an ncomp field; old <- new
+// after the last component.  The convergence measure MESO_RES_L2 selects instead of the reference's
+// mean relative change, which divides by values near zero.
+double residual_l2(const meso_ctx *c, const std::vector<double> &old, const std::vector<double> &nw, int ncomp, int k) {
+    double num = 0.0, den = 0.0;
+    for (int i = 0; i < c->C; ++i) {
+        const double d = nw[(size_t)ncomp * i + k] - old[(size_t)ncomp * i + k], o = old[(size_t)ncomp * i + k];
+        num += c->vol[i] * d * d;
+        den += c->vol[i] * o * o;
+    }
+    return den > 0.0 ? std::sqrt(num / den) : std::sqrt(num);
+}
+
 // Residual check of do_step (e.g. cdugks_shakhov.cpp:729-757).
 int residual_check(meso_ctx *c) {
     std::vector<double> rho, u, T, q;
     int rc = download_macros(c, rho, u, T, q);
     if (rc) return rc;
+    if (c->params.residual_fields & MESO_RES_L2) {
+        const int D = c->dim;
+        std::vector<double> list = {residual_l2(c, c->rho_res, rho, 1, 0)};
+        std::vector<int> field = {MESO_RES_RHO};
+        if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV) list.push_back(residual_l2(c, c->T_res, T, 1, 0)), field.push_back(MESO_RES_T);
+        for (int k = 0; k < D; ++k) list.push_back(residual_l2(c, c->u_res, u, 3, k)), field.push_back(MESO_RES_U);
+        if (c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV)
+            for (int k = 0; k < D; ++k) list.push_back(residual_l2(c, c->q_res, q, 3, k)), field.push_back(MESO_RES_Q);
+        c->rho_res = rho;
+        c->T_res = T;
+        c->u_res = u;
+        c->q_res = q;
+        c->nres = (int)list.size();
+        for (int i = 0; i < c->nres; ++i) c->last_res[i] = list[i];
+        const int watch = c->params.residual_fields & (MESO_RES_RHO | MESO_RES_T | MESO_RES_U | MESO_RES_Q);
+        bool conv = true;
+        for (size_t i = 0; i < list.size(); ++i)
+            if (watch == 0 || (watch & field[i])) conv = conv && (list[i] <= c->params.residual_limit);
+        if (conv) c->converge_state++;
+        else c->converge_state = 0;
+        if (c->converge_state >= 10) {
+            c->run_state = 0;
+            c->converged = 1;
+        }
+        return MESO_OK;
+    }
     double rr = residual_scalar(c, c->rho_res, rho);
     double ru[3];
     residual_vector(c, c->u_res, u, ru);
@@ -405,7 +444,7 @@ int residual_check(meso_ctx *c) {
     }
     c->nres = (int)list.size();
     for (int i = 0; i < c->nres; ++i) c->last_res[i] = list[i];
-    const int watch = c->params.residual_fields;
+    const int watch = c->params.residual_fields & (MESO_RES_RHO | MESO_RES_T | MESO_RES_U | MESO_RES_Q);
     bool conv = true;
     for (size_t i = 0; i < list.size(); ++i)
         if (watch == 0 || (watch & field[i])) conv = conv && (list[i] <= c->params.residual_limit);
@@ -418,7 +457,35 @@ int residual_check(meso_ctx *c) {
     return MESO_OK;
 }
 
+// The FP32 step's launches take no per-step arguments (each instance reads its state parity from
+// its device step counter), so they are captured once as a CUDA graph and replayed.
+bool capture_f32_graph(meso_ctx *c) {
+    if (c->f32_graph) cudaGraphExecDestroy(c->f32_graph);
+    c->f32_graph = nullptr;
+    cudaGraph_t g = nullptr;
+    int64_t n = 0;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+    const int rc = meso::fp32_step(c->fs, c->stream, &n);
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    bool ok = rc == 0 && e == cudaSuccess && cudaGraphInstantiate(&c->f32_graph, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+        cudaGetLastError();
+        c->f32_graph = nullptr;
+        return false;
+    }
+    c->f32_graph_version = c->f32_version;
+    c->f32_graph_launches = n;
+    return true;
+}
+
 int launch_step(meso_ctx *c) {
+    if (c->params.precision == MESO_FP32 && (c->f32_graph_version == c->f32_version || capture_f32_graph(c))) {
+        if (cudaGraphLaunch(c->f32_graph, c->stream) != cudaSuccess)
+            return fail(MESO_ERR_CUDA, std::string("graph launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+        c->last_launches += c->f32_graph_launches;
+        return MESO_OK;
+    }
     int rc = c->params.precision == MESO_FP32 ? meso::fp32_step(c->fs, c->stream, &c->last_launches)
                                               : meso::plain_step(c->ps, c->stream, &c->last_launches);
     if (rc) return fail(MESO_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(cudaGetLastError()));
@@ -717,6 +784,7 @@ void meso_ctx_destroy(meso_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->batch) meso_host::batch_forget(c->batch, c);
+    if (c->f32_graph) cudaGraphExecDestroy(c->f32_graph);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_fp32_launch(c->fs, c->fs_owned);
     c->arena.release();

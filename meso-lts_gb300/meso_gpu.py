@@ -20,7 +20,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_NAN, ERR_TIMEOUT, ERR_IO, ERR_UNSUPPORTE
 SOLVER_DUGKS, SOLVER_CDUGKS, SOLVER_CDUGKS_SHAKHOV = 0, 1, 2
 FP64, FP32 = 0, 1
 NOALLOC_MAX_CELLS = 131072  # MESO_NOALLOC_MAX_CELLS
-RES_RHO, RES_T, RES_U, RES_Q = 1, 2, 4, 8  # MESO_RES_*
+RES_RHO, RES_T, RES_U, RES_Q, RES_L2 = 1, 2, 4, 8, 16  # MESO_RES_*
 BC = dict(fluid_interior=0, farfield_inlet=1, pressure_inlet=2, freestream_inlet=3, farfield_outlet=4,
           pressure_outlet=5, wall=6, slip_wall=7, symmetry=8)
 
