@@ -160,6 +160,11 @@ typedef struct meso_params {
     int32_t residual_fields;     /* fields the convergence test watches: 0 = all the reference watches
                                     (cdugks_shakhov.cpp:747-756), else MESO_RES_* bits; no counterpart
                                     in the reference (served solves converge on U) */
+    /* FP32 kernel shape (0 = the library's choice or the autotuner's cached pick); no counterpart in
+       the reference: cells per tile (8..40), velocities per lane (1 or 2), velocity groups per tile */
+    int32_t tile_cells;
+    int32_t vpl;
+    int32_t ngroup;
     int32_t pad_;
 } meso_params;
 
@@ -299,6 +304,24 @@ int64_t meso_last_step_launches(meso_ctx *ctx);
 int meso_phase_times(meso_ctx *ctx, int32_t nsteps, double *ms, int32_t max_phases, int32_t *nphases);
 /* Kernel name(s) of phase i of this context's step. */
 const char *meso_phase_name(meso_ctx *ctx, int32_t i);
+
+/* ---- FP32 kernel-shape autotuner ---------------------------------------- */
+
+/*
+ * Measures the FP32 step of this solve for each candidate kernel shape (cells
+ * per tile, velocities per lane, velocity groups per tile: meso_params
+ * tile_cells / vpl / ngroup), `steps` timed steps each from a uniform
+ * equilibrium, and returns in *best the params with the fastest shape (and its
+ * time per step in *best_ms, may be NULL).  The shape is remembered for solves
+ * with the same cell, face and velocity counts: contexts created afterwards
+ * with tile_cells = vpl = ngroup = 0 use it.  No counterpart in the reference.
+ */
+int meso_autotune(const meso_mesh_desc *mesh, const meso_dvs_desc *dvs, const meso_mark_desc *marks, int32_t nmarks,
+                  const meso_params *params, int32_t steps, meso_params *best, double *best_ms);
+/* The same for a case file (its mesh, velocity set, marks and settings). */
+int meso_autotune_case(const char *case_file, int32_t steps, meso_params *best, double *best_ms);
+/* Forget every remembered shape. */
+void meso_autotune_forget(void);
 
 /* ---- batched solves ----------------------------------------------------- */
 

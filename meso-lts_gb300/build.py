@@ -26,7 +26,7 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SRCS = ["host/mesh.cpp", "host/config.cpp", "host/case.cpp", "host/renumber.cpp", "host/output.cpp",
-             "host/tiles.cpp", "host/fp32_host.cpp", "capi.cpp", "batch.cpp", "server.cpp"]
+             "host/tiles.cpp", "host/fp32_host.cpp", "capi.cpp", "batch.cpp", "server.cpp", "autotune.cpp"]
 # (source, extra nvcc flags)
 CUDA_SRCS = [("kernels/plain_fp64.cu", ["-fmad=false"]),
              ("kernels/fp32_step.cu", []),

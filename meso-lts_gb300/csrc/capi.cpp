@@ -276,7 +276,7 @@ int build_device(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d) {
             c->ps.solver = c->params.solver;
             c->ps.num_sms = c->num_sms;
             if (meso::fp32_configure(c->device)) return fail(MESO_ERR_CUDA, "FP32 kernel configuration failed");
-            int rc = build_fp32_instance(c, m, d, c->plan, 0);
+            int rc = build_fp32_instance(c, m, d, c->plan, c->params.ngroup, c->params.vpl);
             if (rc) return rc;
             return MESO_OK;
         }
@@ -511,7 +511,8 @@ int refresh_f32(meso_ctx *c) {
 }
 
 bool fp32_fixed_changed(const meso_params &a, const meso_params &b) {
-    return a.R != b.R || a.T0 != b.T0 || a.rho0 != b.rho0 || a.K != b.K || a.limiter_switch != b.limiter_switch;
+    return a.R != b.R || a.T0 != b.T0 || a.rho0 != b.rho0 || a.K != b.K || a.limiter_switch != b.limiter_switch ||
+           a.tile_cells != b.tile_cells || a.vpl != b.vpl || a.ngroup != b.ngroup;
 }
 
 // Live reload of [settings] (cdugks_shakhov.cpp:762): the reference re-reads
@@ -534,6 +535,9 @@ void maybe_reload(meso_ctx *c) {
                 c->params.rho0 = prev.rho0;
                 c->params.K = prev.K;
                 c->params.limiter_switch = prev.limiter_switch;
+                c->params.tile_cells = prev.tile_cells;
+                c->params.vpl = prev.vpl;
+                c->params.ngroup = prev.ngroup;
             }
             derive_kparams(c->params, c->dim, c->ps.kp);
             refresh_f32(c);
@@ -583,7 +587,21 @@ meso_ctx *new_ctx(const meso_mesh_desc *m, const meso_dvs_desc *d, const meso_ma
                        "FP32 storage covers the 2-D Shakhov solver without the limiter; use MESO_FP64");
             return nullptr;
         }
-        if (!plan_fp32(*m, meso::F32_MAX_CELLS, c->rn, c->plan)) {
+        if (c->params.tile_cells == 0 && c->params.vpl == 0 && c->params.ngroup == 0) {
+            int tc = 0, v = 0, ng = 0;  // a shape the autotuner measured for a solve of this size
+            if (tuned_shape(m->ncell, m->nface, d->nv, tc, v, ng)) {
+                c->params.tile_cells = tc;
+                c->params.vpl = v;
+                c->params.ngroup = ng;
+            }
+        }
+        const int T = c->params.tile_cells > 0 ? c->params.tile_cells : meso::F32_MAX_CELLS;
+        if (T < 8 || T > meso::F32_MAX_CELLS || c->params.vpl < 0 || c->params.vpl > meso::F32_MAX_VPL ||
+            c->params.ngroup < 0) {
+            *rc = fail(MESO_ERR_INVALID, "FP32 kernel shape out of range (tile_cells 8..40, vpl 0..2, ngroup >= 0)");
+            return nullptr;
+        }
+        if (!plan_fp32(*m, T, c->rn, c->plan)) {
             *rc = fail(MESO_ERR_UNSUPPORTED, "mesh connectivity exceeds the FP32 tile limits");
             return nullptr;
         }
@@ -933,7 +951,7 @@ int meso_set_params(meso_ctx *c, const meso_params *p) {
     std::string why;
     if (!valid_params(*p, why)) return fail(MESO_ERR_INVALID, why);
     if (c->params.precision == MESO_FP32 && fp32_fixed_changed(c->params, *p))
-        return fail(MESO_ERR_UNSUPPORTED, "the FP32 form fixes R, T0, rho0, K and the limiter switch at creation");
+        return fail(MESO_ERR_UNSUPPORTED, "the FP32 form fixes R, T0, rho0, K, the limiter switch and the kernel shape at creation");
     c->params = *p;
     derive_kparams(c->params, c->dim, c->ps.kp);
     return refresh_f32(c);

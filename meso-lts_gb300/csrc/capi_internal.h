@@ -44,6 +44,7 @@ void derive_kparams(const meso_params &p, int dim, meso::KParams &k);
 int ctx_read_status(meso_ctx *c);    // device status -> c->h_status (syncs the context's stream)
 int ctx_residual_check(meso_ctx *c); // residual + convergence counter of do_step
 void batch_forget(meso_batch *b, meso_ctx *c);  // batch.cpp
+bool tuned_shape(int ncell, int nface, int nv, int &tile_cells, int &vpl, int &ngroup);  // autotune.cpp
 
 }  // namespace meso_host
 

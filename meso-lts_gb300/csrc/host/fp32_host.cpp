@@ -39,11 +39,13 @@ template <class T> T *up(DevArena &A, const std::vector<T> &v, cudaStream_t s) {
 }
 }  // namespace
 
-int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d, const TilePlan &P, int ngroup) {
+int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d, const TilePlan &P, int ngroup,
+                        int vpl_req) {
     auto &A = c->arena;
     auto s = c->stream;
     const int C = m->ncell, F = m->nface, NV = d->nv;
-    const int vpl = NV >= 256 ? 2 : 1;  // small velocity sets keep one velocity per lane
+    // small velocity sets keep one velocity per lane unless asked otherwise
+    const int vpl = vpl_req == 1 || vpl_req == 2 ? vpl_req : (NV >= 256 ? 2 : 1);
     const int NVp = (NV + 32 * vpl - 1) / (32 * vpl) * (32 * vpl);
     const auto &rn = c->rn;
     meso::F32Inst I;

@@ -22,7 +22,7 @@ bool plan_fp32(const meso_mesh_desc &m, int tile_cells, Renumbering &rn, TilePla
 
 // Allocates and uploads the instance of context c (c->rn must be the tiled renumbering).
 int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d, const TilePlan &plan,
-                        int ngroup);
+                        int ngroup, int vpl = 0);
 
 // Launch state over a list of instances (device copies of their F32Inst + work items).
 int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso::Fp32State &s,

@@ -55,7 +55,8 @@ class Params(C.Structure):
                 ("dt", C.c_double), ("R", C.c_double), ("T0", C.c_double), ("rho0", C.c_double),
                 ("L0", C.c_double), ("mu0", C.c_double), ("vhs_index", C.c_double), ("Pr", C.c_double),
                 ("Ma", C.c_double), ("Re", C.c_double), ("CFL", C.c_double), ("venkata_k", C.c_double),
-                ("residual_limit", C.c_double), ("residual_fields", C.c_int32), ("pad_", C.c_int32)]
+                ("residual_limit", C.c_double), ("residual_fields", C.c_int32), ("tile_cells", C.c_int32),
+                ("vpl", C.c_int32), ("ngroup", C.c_int32), ("pad_", C.c_int32)]
 
 
 class Status(C.Structure):
@@ -112,6 +113,10 @@ _SIGS = {
     "meso_batch_size": (C.c_int32, [C.c_void_p]),
     "meso_batch_last_step_ms": (C.c_double, [C.c_void_p]),
     "meso_batch_last_step_launches": (C.c_int64, [C.c_void_p]),
+    "meso_autotune": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(DvsDesc), C.POINTER(MarkDesc), C.c_int32,
+                                 C.POINTER(Params), C.c_int32, C.POINTER(Params), _dp]),
+    "meso_autotune_case": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(Params), _dp]),
+    "meso_autotune_forget": (None, []),
     "meso_server_create": (C.c_int, [C.c_int64, C.c_int32, C.POINTER(C.c_void_p)]),
     "meso_server_destroy": (None, [C.c_void_p]),
     "meso_server_submit": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.POINTER(C.c_int64)]),
@@ -428,3 +433,11 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def autotune(case_path: str, steps: int = 5) -> tuple:
+    """FP32 kernel shape measured for a case file: (Params with tile_cells / vpl / ngroup, ms per step)."""
+    best = Params()
+    ms = np.zeros(1)
+    _check(lib().meso_autotune_case(os.fsencode(case_path), steps, C.byref(best), _ptr(ms)))
+    return best, float(ms[0])
