@@ -595,7 +595,7 @@ meso_ctx *new_ctx(const meso_mesh_desc *m, const meso_dvs_desc *d, const meso_ma
                 c->params.ngroup = ng;
             }
         }
-        const int T = c->params.tile_cells > 0 ? c->params.tile_cells : meso::F32_MAX_CELLS;
+        const int T = c->params.tile_cells > 0 ? c->params.tile_cells : meso::F32_DEFAULT_CELLS;
         if (T < 8 || T > meso::F32_MAX_CELLS || c->params.vpl < 0 || c->params.vpl > meso::F32_MAX_VPL ||
             c->params.ngroup < 0) {
             *rc = fail(MESO_ERR_INVALID, "FP32 kernel shape out of range (tile_cells 8..40, vpl 0..2, ngroup >= 0)");

@@ -185,38 +185,18 @@ __device__ __forceinline__ int find_inst(const int *off, int n, int g) {
     return lo;
 }
 
-// ---- TMA bulk copies and mbarriers (PTX ISA 8.0+, sm_90 and later) --------
+// ---- asynchronous global -> shared copies (cp.async, sm_80 and later) -------------
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
-__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+// 16 bytes from global to shared, completing with the thread's current commit group.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// One 256-byte velocity-contiguous segment (32 float2) from global to shared, completing on `bar`.
-__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-// Bounded wait: each try_wait suspends up to a hardware time limit; 2^22 tries is far beyond any copy.
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
-    for (int i = 0; i < (1 << 22); ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Waits until at most N of the thread's commit groups are still in flight.
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 struct OwnedFace {     // P1: one face owned by the tile
@@ -236,13 +216,12 @@ struct CellFace {      // P2: one face of a tile cell, seen from that cell
 
 template <int VPL> struct __align__(128) TileSmem {
     static constexpr int SEG = 32 * VPL;         // velocities of one slot in a chunk
-    float2 phi[2][F32_MAX_SLOTS * SEG];         // double-buffered chunk of the tile + halo (bulk-copy target)
+    float2 phi[2][F32_MAX_SLOTS * SEG];         // double-buffered chunk of the tile + halo (cp.async target)
     float4 G[F32_MAX_GSLOTS * SEG];             // gradients (g_x, g_y, h_x, h_y) of tile + 1-ring cells
     float2 ga[F32_MAX_GENT];                    // gradient stencil coefficients
     int slot_cell[F32_MAX_SLOTS];
     unsigned short gnbr[F32_MAX_GENT];
     unsigned short gptr[F32_MAX_GSLOTS + 1];
-    unsigned long long mbar[2];
     int nS, nG, nX, base;
     union {
         struct {
@@ -281,20 +260,32 @@ template <int VPL> __device__ __forceinline__ void stage_common(const F32Inst &I
     }
 }
 
-// Warp 0 issues the bulk copies of chunk `ch` (32 VPL velocities of every slot) into phi[buf].
+// Every thread issues 16-byte asynchronous copies of chunk `ch` (32 VPL velocities of every slot)
+// into phi[buf]; a warp instruction covers 512 contiguous bytes of one or two slots.  One commit
+// group per chunk.  Spreading the copies over all threads keeps any one warp from stalling on them.
 template <int VPL>
-__device__ __forceinline__ void issue_chunk(const float2 *S, int NVp, int ch, int buf, TileSmem<VPL> &sm) {
+__device__ __forceinline__ void load_chunk(const float2 *S, int NVp, int ch, int buf, TileSmem<VPL> &sm) {
     constexpr int SEG = TileSmem<VPL>::SEG;
-    const int lane = threadIdx.x & 31;
-    const int nS = sm.nS;
-    if (lane == 0) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(&sm.mbar[buf], (unsigned)nS * (unsigned)(SEG * 8));
+    constexpr int PER = SEG / 2;  // 16-byte pieces of one slot's segment
+    const int n = sm.nS * PER;
+    for (int i = threadIdx.x; i < n; i += kT) {
+        const int s = i / PER, k = i - s * PER;
+        cp_async16(&sm.phi[buf][s * SEG + 2 * k], S + (size_t)sm.slot_cell[s] * NVp + (size_t)ch * SEG + 2 * k);
     }
-    __syncwarp();
-    for (int s = lane; s < nS; s += 32)
-        bulk_load(&sm.phi[buf][s * SEG], S + (size_t)sm.slot_cell[s] * NVp + (size_t)ch * SEG, SEG * 8u,
-                  &sm.mbar[buf]);
+    cp_async_commit();
+}
+
+// Makes chunk `ch` (issued one iteration earlier) visible to the CTA and starts the copies of chunk
+// ch + 1 into the other buffer, which the previous iteration has finished reading.
+template <int VPL>
+__device__ __forceinline__ void next_chunk(const float2 *S, int NVp, int ch, int ch1, int buf, TileSmem<VPL> &sm) {
+    if (ch + 1 < ch1) {
+        load_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
+        cp_async_wait<1>();
+    } else {
+        cp_async_wait<0>();
+    }
+    __syncthreads();
 }
 
 // Gradients of the first nG slots from phi[buf].
@@ -383,28 +374,6 @@ __device__ __forceinline__ float warp_sum16(float (&v)[16], int lane) {
     return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
 }
 
-// Records a timed-out wait; the CTA then drains its own copies (bounded) and leaves the kernel.
-template <int VPL>
-__device__ __forceinline__ bool wait_or_bail(TileSmem<VPL> &sm, int buf, unsigned parity, DStatus *st) {
-    const bool ok = mbar_wait(&sm.mbar[buf], parity);
-    if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) atomicExch(&st->timeout, 1);
-        mbar_wait(&sm.mbar[buf], parity);
-        mbar_wait(&sm.mbar[buf ^ 1], parity ^ 1u);
-        return false;
-    }
-    return true;
-}
-
-template <int VPL> __device__ __forceinline__ void init_barriers(TileSmem<VPL> &sm) {
-    if (threadIdx.x == 0) {
-        mbar_init(&sm.mbar[0], 1);
-        mbar_init(&sm.mbar[1], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-}
-
 // =============================================================================
 // P1: raw face moments
 // =============================================================================
@@ -415,8 +384,6 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
     extern __shared__ float4 smem_raw[];
     TileSmem<VPL> &sm = *reinterpret_cast<TileSmem<VPL> *>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    init_barriers(sm);
-    unsigned use0 = 0u, use1 = 0u;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 item = items[it];
         const F32Inst &I = insts[item.x];
@@ -453,13 +420,10 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
         }
         for (int k = threadIdx.x; k < nOF * 22; k += kT) sm.u.p1.acc[k] = 0.f;
         __syncthreads();
-        if (warp == 0) issue_chunk<VPL>(S, NVp, ch0, 0, sm);
+        load_chunk<VPL>(S, NVp, ch0, 0, sm);
         for (int ch = ch0; ch < ch1; ++ch) {
             const int buf = (ch - ch0) & 1;
-            if (warp == 0 && ch + 1 < ch1) issue_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
-            if (!wait_or_bail(sm, buf, (buf ? use1 : use0) & 1u, I.status)) return;
-            if (buf) ++use1;
-            else ++use0;
+            next_chunk<VPL>(S, NVp, ch, ch1, buf, sm);
             gradients(sm, buf, grad_on);
             __syncthreads();
             float xx[VPL], xy[VPL], w[VPL], hx[VPL], hy[VPL];
@@ -524,8 +488,6 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
     extern __shared__ float4 smem_raw[];
     TileSmem<VPL> &sm = *reinterpret_cast<TileSmem<VPL> *>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    init_barriers(sm);
-    unsigned use0 = 0u, use1 = 0u;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 item = items[it];
         const F32Inst &I = insts[item.x];
@@ -577,13 +539,10 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         }
         for (int k = threadIdx.x; k < nc * 4; k += kT) sm.u.p2.acc[k] = 0.f;
         __syncthreads();
-        if (warp == 0) issue_chunk<VPL>(S, NVp, ch0, 0, sm);
+        load_chunk<VPL>(S, NVp, ch0, 0, sm);
         for (int ch = ch0; ch < ch1; ++ch) {
             const int buf = (ch - ch0) & 1;
-            if (warp == 0 && ch + 1 < ch1) issue_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
-            if (!wait_or_bail(sm, buf, (buf ? use1 : use0) & 1u, I.status)) return;
-            if (buf) ++use1;
-            else ++use0;
+            next_chunk<VPL>(S, NVp, ch, ch1, buf, sm);
             gradients(sm, buf, grad_on);
             __syncthreads();
             float xx[VPL], xy[VPL], w[VPL], hx[VPL], hy[VPL], g0[VPL], x2[VPL];

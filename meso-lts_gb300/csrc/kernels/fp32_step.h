@@ -21,6 +21,7 @@ constexpr int F32_MAX_GSLOTS = 72;  // tile + one-ring halo cells (gradients)
 constexpr int F32_MAX_GENT = 432;   // gradient stencil entries per tile
 constexpr int F32_MAX_OWNED = 100;  // faces owned by a tile
 constexpr int F32_MAX_CELLS = 40;   // cells per tile
+constexpr int F32_DEFAULT_CELLS = 32;  // tile size without an autotuned shape (two cells per warp)
 constexpr int F32_MAX_CF = 160;     // cell-face entries per tile (tile cells x faces per cell)
 constexpr int F32_NMOM = 11;        // raw face moments about the reference velocity (2-D)
 
