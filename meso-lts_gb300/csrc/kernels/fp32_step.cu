@@ -39,6 +39,7 @@
 // lies within a rounding margin of zero.  Per-face and per-cell scalar work
 // (pow, divisions) runs one thread per face / cell in FP64.
 #include <cfloat>
+#include <cstddef>
 #include <climits>
 
 #include "fp32_step.h"
@@ -238,6 +239,8 @@ template <int VPL> struct __align__(128) TileSmem {
 };
 
 template <int VPL> constexpr size_t tile_smem() { return sizeof(TileSmem<VPL>); }
+// cp.async destinations must be 16-byte aligned
+static_assert(offsetof(TileSmem<1>, phi) % 16 == 0 && offsetof(TileSmem<2>, phi) % 16 == 0, "phi alignment");
 static_assert(sizeof(TileSmem<F32_MAX_VPL>) <= 227 * 1024, "tile staging exceeds the shared memory of one CTA");
 
 // Per-item staging of the slot list and the gradient stencil.
