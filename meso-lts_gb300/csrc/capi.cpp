@@ -598,7 +598,8 @@ meso_ctx *new_ctx(const meso_mesh_desc *m, const meso_dvs_desc *d, const meso_ma
         const int T = c->params.tile_cells > 0 ? c->params.tile_cells : meso::F32_DEFAULT_CELLS;
         if (T < 8 || T > meso::F32_MAX_CELLS || c->params.vpl < 0 || c->params.vpl > meso::F32_MAX_VPL ||
             c->params.ngroup < 0) {
-            *rc = fail(MESO_ERR_INVALID, "FP32 kernel shape out of range (tile_cells 8..40, vpl 0..2, ngroup >= 0)");
+            *rc = fail(MESO_ERR_INVALID, "FP32 kernel shape out of range (tile_cells 8.." +
+                                             std::to_string(meso::F32_MAX_CELLS) + ", vpl 0..2, ngroup >= 0)");
             return nullptr;
         }
         if (!plan_fp32(*m, T, c->rn, c->plan)) {

@@ -17,7 +17,8 @@ bool plan_fp32(const meso_mesh_desc &m, int tile_cells, Renumbering &rn, TilePla
         rn = renumber_tiled(m, T, sizes);
         if (build_tile_plan(m, rn, sizes, meso::F32_MAX_SLOTS, meso::F32_MAX_GSLOTS, meso::F32_MAX_OWNED,
                             meso::F32_MAX_CELLS, plan) &&
-            plan.max_gentries <= meso::F32_MAX_GENT && plan.max_cf <= meso::F32_MAX_CF)
+            plan.max_gentries <= meso::F32_MAX_GENT && plan.max_cf <= meso::F32_MAX_CF &&
+            plan.max_tf <= meso::F32_MAX_TF)
             return true;
     }
     return false;
@@ -145,7 +146,11 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.tile_fstart = up(A, P.tile_fstart, s);
         I.face_own_slot = up(A, P.face_own_slot, s);
         I.face_nei_slot = up(A, P.face_nei_slot, s);
-        I.cf_oslot = up(A, P.cf_oslot, s);
+        I.tile_tf_ptr = up(A, P.tile_tf_ptr, s);
+        I.tf_face = up(A, P.tf_face, s);
+        I.tf_os = up(A, P.tf_os, s);
+        I.tf_ns = up(A, P.tf_ns, s);
+        I.cf_tf = up(A, P.cf_tf, s);
         I.cf_ptr = c->dm.cf_ptr;
         I.cf_face = c->dm.cf_face;
         I.fown = up(A, fown, s);
@@ -172,6 +177,9 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.xi64y = up(A, xy64, s);
         I.w64 = up(A, w64, s);
         I.g0_32 = up(A, g032, s);
+        std::vector<float4> vt(NVp);
+        for (int q = 0; q < NVp; ++q) vt[q] = make_float4(xx[q], xy[q], w[q], g032[q]);
+        I.vt32 = up(A, vt, s);
         I.g0_64 = up(A, g064, s);
         I.sym = up(A, sym, s);
         const size_t cv = (size_t)C * NVp;

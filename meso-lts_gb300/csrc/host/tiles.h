@@ -18,6 +18,7 @@ namespace meso_host {
 
 struct TilePlan {
     int ntile = 0, max_cells = 0, max_slots = 0, max_gslots = 0, max_owned = 0, max_gentries = 0, max_cf = 0;
+    int max_tf = 0;
     std::vector<int> tile_cstart, tile_ncell;        // [ntile]
     std::vector<int> tile_slot_ptr, slot_cell;       // slots: tile cells, 1-ring halo, 2-ring halo
     std::vector<int> tile_gslots;                    // [ntile] slots with a gradient (tile + 1-ring)
@@ -28,6 +29,12 @@ struct TilePlan {
     std::vector<int> tile_fstart;                    // [ntile+1] owned face range
     std::vector<uint16_t> face_own_slot, face_nei_slot;  // per face, in its owner tile
     std::vector<uint16_t> cf_oslot;                  // per cell-face entry: slot of the other cell in the cell's tile
+    // faces that touch a tile cell, each once per tile (the update kernel evaluates each once)
+    std::vector<int> tile_tf_ptr;                    // [ntile+1]
+    std::vector<int> tf_face;                        // renumbered face id
+    std::vector<uint16_t> tf_os, tf_ns;              // slots of the face's owner and neighbour
+    std::vector<uint8_t> cf_tf;                      // per cell-face entry: tile-face index, | 0x80 when the cell
+                                                     // is the face's neighbour (flux counted negative)
 };
 
 // Renumbering that tiles the mesh (cells grouped by tile, faces by owner).

@@ -206,13 +206,12 @@ struct OwnedFace {     // P1: one face owned by the tile
     unsigned short os, ns;
     int pad;
 };
-struct CellFace {      // P2: one face of a tile cell, seen from that cell
+struct TileFace {      // P2: one face touching a tile cell (evaluated once per chunk)
     FaceK fk;
     float2 n, fdo, fdn;
-    float area_s;      // +area if the cell owns the face, -area otherwise
+    float area;
     int bnd, face;
-    unsigned short oslot;
-    unsigned char own, pad;
+    unsigned short os, ns;  // slots of the owner and the neighbour
 };
 
 template <int VPL> struct __align__(128) TileSmem {
@@ -230,10 +229,13 @@ template <int VPL> struct __align__(128) TileSmem {
             float acc[F32_MAX_OWNED * 22];
         } p1;
         struct {
+            float2 ff[F32_MAX_TF * SEG];        // (n0.xi) A f_face of each tile face, this chunk
             CellK ck[F32_MAX_CELLS];
-            CellFace cf[F32_MAX_CF];
+            TileFace tf[F32_MAX_TF];
             int cf_off[F32_MAX_CELLS + 1];
             float acc[F32_MAX_CELLS * 4];
+            unsigned char cft[F32_MAX_CF];      // per cell-face entry: tile face | 0x80 if the cell is its neighbour
+            int ntf;
         } p2;
     } u;
 };
@@ -401,9 +403,7 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
         const int NVp = I.NVp;
         const float hdt = (float)I.hdt;
         const int grad_on = I.gradient;
-        const float *__restrict__ xi32x = I.xi32x;
-        const float *__restrict__ xi32y = I.xi32y;
-        const float *__restrict__ w32 = I.w32;
+        const float4 *__restrict__ vt32 = I.vt32;
         float2 *__restrict__ bnd_in = I.bnd_in;
         stage_common(I, tile, sm);
         for (int f = threadIdx.x; f < nOF; f += kT) {
@@ -434,9 +434,10 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
 #pragma unroll
             for (int v = 0; v < VPL; ++v) {
                 p[v] = ch * SEG + v * 32 + lane;
-                xx[v] = xi32x[p[v]];
-                xy[v] = xi32y[p[v]];
-                w[v] = w32[p[v]];
+                const float4 t = vt32[p[v]];
+                xx[v] = t.x;
+                xy[v] = t.y;
+                w[v] = t.z;
                 hx[v] = hdt * xx[v];
                 hy[v] = hdt * xy[v];
             }
@@ -507,38 +508,28 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         const float hdt = (float)I.hdt;
         const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
         const int grad_on = I.gradient;
-        const float *__restrict__ xi32x = I.xi32x;
-        const float *__restrict__ xi32y = I.xi32y;
-        const float *__restrict__ w32 = I.w32;
-        const float *__restrict__ g0_32 = I.g0_32;
+        const float4 *__restrict__ vt32 = I.vt32;
         const float2 *__restrict__ bnd_out = I.bnd_out;
         stage_common(I, tile, sm);
         const int j0 = I.cf_ptr[cs];
         for (int c = threadIdx.x; c < nc; c += kT) sm.u.p2.ck[c] = I.ck[cs + c];
         for (int c = threadIdx.x; c <= nc; c += kT) sm.u.p2.cf_off[c] = I.cf_ptr[cs + c] - j0;
         const int ncf = I.cf_ptr[cs + nc] - j0;
-        for (int e = threadIdx.x; e < ncf; e += kT) {
-            const int j = j0 + e;
-            const int f = I.cf_face[j];
-            int lo = 0, hi = nc;  // the tile cell whose face list holds entry j
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (I.cf_ptr[cs + mid] <= j) lo = mid;
-                else hi = mid;
-            }
-            const bool own = I.fown[f] == cs + lo;
-            CellFace x;
+        for (int e = threadIdx.x; e < ncf; e += kT) sm.u.p2.cft[e] = I.cf_tf[j0 + e];
+        const int q0 = I.tile_tf_ptr[tile], ntf = I.tile_tf_ptr[tile + 1] - q0;
+        for (int q = threadIdx.x; q < ntf; q += kT) {
+            const int f = I.tf_face[q0 + q];
+            TileFace x;
             x.n = I.fn32[f];
             x.fdo = I.fdo[f];
             x.fdn = I.fdn[f];
-            x.area_s = own ? I.farea[f] : -I.farea[f];
+            x.area = I.farea[f];
             x.bnd = I.fbnd[f];
             x.face = f;
-            x.oslot = I.cf_oslot[j];
-            x.own = own ? 1 : 0;
-            x.pad = 0;
+            x.os = I.tf_os[q0 + q];
+            x.ns = I.tf_ns[q0 + q];
             if (x.bnd < 0) x.fk = I.fk[f];
-            sm.u.p2.cf[e] = x;
+            sm.u.p2.tf[q] = x;
         }
         for (int k = threadIdx.x; k < nc * 4; k += kT) sm.u.p2.acc[k] = 0.f;
         __syncthreads();
@@ -553,46 +544,58 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
 #pragma unroll
             for (int v = 0; v < VPL; ++v) {
                 p[v] = ch * SEG + v * 32 + lane;
-                xx[v] = xi32x[p[v]];
-                xy[v] = xi32y[p[v]];
+                const float4 t = vt32[p[v]];
+                xx[v] = t.x;
+                xy[v] = t.y;
                 x2[v] = fmaf(xx[v], xx[v], xy[v] * xy[v]);
-                w[v] = w32[p[v]];
-                g0[v] = g0_32[p[v]];
+                w[v] = t.z;
+                g0[v] = t.w;
                 hx[v] = hdt * xx[v];
                 hy[v] = hdt * xy[v];
             }
+            // each face touching a tile cell, once: its flux value (n0.xi) A f_face, seen from the owner
+            for (int q = warp; q < ntf; q += F32_WARPS) {
+                const TileFace &x = sm.u.p2.tf[q];
+                float2 *ff = sm.u.p2.ff + q * SEG + lane;
+                const float2 n = x.n;
+                const float area = x.area;
+                if (x.bnd >= 0) {
+                    const float2 *bo = bnd_out + (size_t)x.bnd * NVp;
+#pragma unroll
+                    for (int v = 0; v < VPL; ++v) {
+                        const float knA = fmaf(n.x, xx[v], n.y * xy[v]) * area;
+                        const float2 gf = bo[p[v]];
+                        ff[v * 32] = make_float2(knA * gf.x, knA * gf.y);
+                    }
+                } else {
+                    const FaceK k = x.fk;
+                    const float2 fdo = x.fdo, fdn = x.fdn;
+#pragma unroll
+                    for (int v = 0; v < VPL; ++v) {
+                        const float d = fmaf(n.x, xx[v], n.y * xy[v]);
+                        const int cls = classify(I, x.face, p[v], d, xx[v], xy[v]);
+                        const float2 gb = face_bar(sm, buf, v, cls, x.os, x.ns, fdo, fdn, hx[v], hy[v]);
+                        const float2 gs = dshakhov(k.e, xx[v], xy[v], x2[v], g0[v], k3, twoK);
+                        const float knA = d * area;
+                        ff[v * 32] = make_float2(knA * fmaf(k.oCs, gb.x, k.Cs * gs.x), knA * fmaf(k.oCs, gb.y, k.Cs * gs.y));
+                    }
+                }
+            }
+            __syncthreads();
             for (int cl = warp; cl < nc; cl += F32_WARPS) {
                 float fg[VPL], fh[VPL];
 #pragma unroll
                 for (int v = 0; v < VPL; ++v) fg[v] = fh[v] = 0.f;
                 const int e1 = sm.u.p2.cf_off[cl + 1];
-                for (int e = sm.u.p2.cf_off[cl]; e < e1; ++e) {
-                    const CellFace &x = sm.u.p2.cf[e];
-                    const float2 n = x.n;
-                    const float area_s = x.area_s;
-                    if (x.bnd >= 0) {
-                        const float2 *bo = bnd_out + (size_t)x.bnd * NVp;
+                for (int e = sm.u.p2.cf_off[cl]; e < e1; ++e) {  // outward flux of the cell
+                    const unsigned char t = sm.u.p2.cft[e];
+                    const float2 *ff = sm.u.p2.ff + (t & 0x7f) * SEG + lane;
+                    const float sgn = (t & 0x80) ? -1.f : 1.f;
 #pragma unroll
-                        for (int v = 0; v < VPL; ++v) {
-                            const float knA = fmaf(n.x, xx[v], n.y * xy[v]) * area_s;
-                            const float2 gf = bo[p[v]];
-                            fg[v] = fmaf(knA, gf.x, fg[v]);
-                            fh[v] = fmaf(knA, gf.y, fh[v]);
-                        }
-                    } else {
-                        const int os = x.own ? cl : x.oslot, ns = x.own ? x.oslot : cl;
-                        const FaceK k = x.fk;
-                        const float2 fdo = x.fdo, fdn = x.fdn;
-#pragma unroll
-                        for (int v = 0; v < VPL; ++v) {
-                            const float d = fmaf(n.x, xx[v], n.y * xy[v]);
-                            const int cls = classify(I, x.face, p[v], d, xx[v], xy[v]);
-                            const float2 gb = face_bar(sm, buf, v, cls, os, ns, fdo, fdn, hx[v], hy[v]);
-                            const float2 gs = dshakhov(k.e, xx[v], xy[v], x2[v], g0[v], k3, twoK);
-                            const float knA = d * area_s;
-                            fg[v] = fmaf(knA, fmaf(k.oCs, gb.x, k.Cs * gs.x), fg[v]);
-                            fh[v] = fmaf(knA, fmaf(k.oCs, gb.y, k.Cs * gs.y), fh[v]);
-                        }
+                    for (int v = 0; v < VPL; ++v) {
+                        const float2 val = ff[v * 32];
+                        fg[v] = fmaf(sgn, val.x, fg[v]);
+                        fh[v] = fmaf(sgn, val.y, fh[v]);
                     }
                 }
                 const CellK k = sm.u.p2.ck[cl];
@@ -715,15 +718,18 @@ __global__ void __launch_bounds__(256) k32_face_eqflux(const F32Inst *__restrict
         const FaceK k = I.fk[f];
         const float2 n = I.fn32[f];
         const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
+        const float4 *__restrict__ vt32 = I.vt32;
         // plain FP32 sums over blocks of 8 velocities per lane, compensated across blocks
         float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
         for (int p0 = 0; p0 < I.NVp; p0 += 32 * 8) {
             float b[4] = {0.f, 0.f, 0.f, 0.f};
             const int pe = min(I.NVp, p0 + 32 * 8);
+#pragma unroll 2
             for (int p = p0 + lane; p < pe; p += 32) {
-                const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
+                const float4 t = vt32[p];
+                const float xx = t.x, xy = t.y, w = t.z;
                 const float x2 = fmaf(xx, xx, xy * xy);
-                const float2 gs = dshakhov(k.e, xx, xy, x2, I.g0_32[p], k3, twoK);
+                const float2 gs = dshakhov(k.e, xx, xy, x2, t.w, k3, twoK);
                 const float wkn = w * fmaf(n.x, xx, n.y * xy);
                 const float a = wkn * gs.x;
                 b[0] += a;

@@ -16,13 +16,14 @@ namespace meso {
 // Kernel limits (the tile planner shrinks tiles until every tile fits).
 constexpr int F32_WARPS = 16;       // warps per CTA of the tile kernels
 constexpr int F32_MAX_VPL = 2;      // velocities per lane (a chunk is 32 x VPL velocities)
-constexpr int F32_MAX_SLOTS = 104;  // tile + two-ring halo cells
-constexpr int F32_MAX_GSLOTS = 72;  // tile + one-ring halo cells (gradients)
-constexpr int F32_MAX_GENT = 432;   // gradient stencil entries per tile
-constexpr int F32_MAX_OWNED = 100;  // faces owned by a tile
-constexpr int F32_MAX_CELLS = 40;   // cells per tile
+constexpr int F32_MAX_SLOTS = 92;   // tile + two-ring halo cells
+constexpr int F32_MAX_GSLOTS = 64;  // tile + one-ring halo cells (gradients)
+constexpr int F32_MAX_GENT = 352;   // gradient stencil entries per tile
+constexpr int F32_MAX_OWNED = 84;   // faces owned by a tile
+constexpr int F32_MAX_CELLS = 32;   // cells per tile
 constexpr int F32_DEFAULT_CELLS = 32;  // tile size without an autotuned shape (two cells per warp)
-constexpr int F32_MAX_CF = 160;     // cell-face entries per tile (tile cells x faces per cell)
+constexpr int F32_MAX_CF = 132;     // cell-face entries per tile (tile cells x faces per cell)
+constexpr int F32_MAX_TF = 84;      // faces touching a tile cell (< 128: indices fit 7 bits)
 constexpr int F32_NMOM = 11;        // raw face moments about the reference velocity (2-D)
 
 // Scalars of one Shakhov equilibrium (rho, u, T, q) for FP32 evaluation of its
@@ -68,7 +69,10 @@ struct F32Inst {
     const uint16_t *gs_nbr;
     const float *gs_ax, *gs_ay;
     const int *tile_fstart;
-    const uint16_t *face_own_slot, *face_nei_slot, *cf_oslot;
+    const uint16_t *face_own_slot, *face_nei_slot;
+    const int *tile_tf_ptr, *tf_face;
+    const uint16_t *tf_os, *tf_ns;
+    const uint8_t *cf_tf;
     // mesh (renumbered)
     const int *cf_ptr, *cf_face, *fown, *fnei, *fbnd, *bface, *fmark;
     const float2 *fn32, *fdo, *fdn;
@@ -83,6 +87,7 @@ struct F32Inst {
     const float *xi32x, *xi32y, *w32;
     const double *xi64x, *xi64y, *w64;
     const float *g0_32;    // [NVp] reference Maxwellian (0 on padding)
+    const float4 *vt32;    // [NVp] (xi_x, xi_y, w, g0) packed for one 16-byte load
     const double *g0_64;
     const int *sym;
     // state and work buffers
