@@ -194,6 +194,7 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.bnd_in = A.alloc<float2>((size_t)std::max(I.nb, 1) * NVp);
         I.bnd_out = A.alloc<float2>((size_t)std::max(I.nb, 1) * NVp);
         I.bnd_g0 = A.alloc<double>(2 * (size_t)std::max(I.nb, 1));
+        I.fbar = A.alloc<float2>((size_t)F * NVp);
         I.ck = A.alloc<meso::CellK>(C);
         I.qpart = A.alloc<double>((size_t)I.ngroup * C * 2);
         I.rho = A.alloc<double>(C);

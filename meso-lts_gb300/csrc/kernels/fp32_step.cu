@@ -206,12 +206,12 @@ struct OwnedFace {     // P1: one face owned by the tile
     unsigned short os, ns;
     int pad;
 };
-struct TileFace {      // P2: one face touching a tile cell (evaluated once per chunk)
+struct UpdFace {       // P2: one face touching a tile cell (evaluated once per chunk)
     FaceK fk;
-    float2 n, fdo, fdn;
+    const float2 *src;  // its reconstructed (interior) or final (boundary) values, [NVp]
+    float2 n;
     float area;
-    int bnd, face;
-    unsigned short os, ns;  // slots of the owner and the neighbour
+    int bnd;
 };
 
 template <int VPL> struct __align__(128) TileSmem {
@@ -228,19 +228,30 @@ template <int VPL> struct __align__(128) TileSmem {
             OwnedFace of[F32_MAX_OWNED];
             float acc[F32_MAX_OWNED * 22];
         } p1;
-        struct {
-            float2 ff[F32_MAX_TF * SEG];        // (n0.xi) A f_face of each tile face, this chunk
-            CellK ck[F32_MAX_CELLS];
-            TileFace tf[F32_MAX_TF];
-            int cf_off[F32_MAX_CELLS + 1];
-            float acc[F32_MAX_CELLS * 4];
-            unsigned char cft[F32_MAX_CF];      // per cell-face entry: tile face | 0x80 if the cell is its neighbour
-            int ntf;
-        } p2;
+
     } u;
 };
 
 template <int VPL> constexpr size_t tile_smem() { return sizeof(TileSmem<VPL>); }
+
+// Shared memory of the update kernel: the tile's cells and the face values of every face touching
+// them, one chunk at a time (no halo, no gradients: the moments kernel stored each face's
+// reconstruction).
+template <int VPL> struct __align__(128) UpdSmem {
+    static constexpr int SEG = 32 * VPL;
+    float2 phi[2][F32_MAX_CELLS * SEG];         // tile cells (cp.async target)
+    float2 fv[2][F32_MAX_TF * SEG];             // face values (cp.async target)
+    float2 ff[F32_MAX_TF * SEG];                // (n0.xi) A f_face of each tile face, this chunk
+    CellK ck[F32_MAX_CELLS];
+    UpdFace uf[F32_MAX_TF];
+    int cf_off[F32_MAX_CELLS + 1];
+    float acc[F32_MAX_CELLS * 4];
+    unsigned char cft[F32_MAX_CF];              // per cell-face entry: tile face | 0x80 if the cell is its neighbour
+    int nc, ntf, cs;
+};
+template <int VPL> constexpr size_t upd_smem() { return sizeof(UpdSmem<VPL>); }
+static_assert(offsetof(UpdSmem<1>, fv) % 16 == 0 && offsetof(UpdSmem<2>, fv) % 16 == 0, "fv alignment");
+static_assert(sizeof(UpdSmem<F32_MAX_VPL>) <= 227 * 1024, "update staging exceeds the shared memory of one CTA");
 // cp.async destinations must be 16-byte aligned
 static_assert(offsetof(TileSmem<1>, phi) % 16 == 0 && offsetof(TileSmem<2>, phi) % 16 == 0, "phi alignment");
 static_assert(sizeof(TileSmem<F32_MAX_VPL>) <= 227 * 1024, "tile staging exceeds the shared memory of one CTA");
@@ -405,6 +416,7 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
         const int grad_on = I.gradient;
         const float4 *__restrict__ vt32 = I.vt32;
         float2 *__restrict__ bnd_in = I.bnd_in;
+        float2 *__restrict__ fbar = I.fbar;
         stage_common(I, tile, sm);
         for (int f = threadIdx.x; f < nOF; f += kT) {
             const int g = fs + f;
@@ -451,6 +463,7 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
                     const int cls = classify(I, o.face, p[v], fmaf(o.n.x, xx[v], o.n.y * xy[v]), xx[v], xy[v]);
                     const float2 gb = face_bar(sm, buf, v, cls, o.os, o.ns, o.fdo, o.fdn, hx[v], hy[v]);
                     if (o.bnd >= 0) bnd_in[(size_t)o.bnd * NVp + p[v]] = gb;
+                    else fbar[(size_t)o.face * NVp + p[v]] = gb;  // read by the update kernel
                     const float c0x = xx[v] - o.u0.x, c0y = xy[v] - o.u0.y;
                     const float wg = w[v] * gb.x, wh = w[v] * gb.y;
                     const float cc = fmaf(c0x, c0x, c0y * c0y);
@@ -485,12 +498,28 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
 // =============================================================================
 // P2: face values, flux, evolution, heat-flux partials
 // =============================================================================
+// Copies of chunk `ch` of the tile's cells and of its faces' values into buffer `buf`, 16 bytes per
+// thread, one commit group.
+template <int VPL>
+__device__ __forceinline__ void load_upd_chunk(const float2 *S, int NVp, int ch, int buf, UpdSmem<VPL> &sm) {
+    constexpr int SEG = UpdSmem<VPL>::SEG, PER = SEG / 2;
+    const int nc = sm.nc, ntf = sm.ntf;
+    for (int i = threadIdx.x; i < (nc + ntf) * PER; i += kT) {
+        const int s = i / PER, k = i - s * PER;
+        if (s < nc)
+            cp_async16(&sm.phi[buf][s * SEG + 2 * k], S + (size_t)(sm.cs + s) * NVp + (size_t)ch * SEG + 2 * k);
+        else
+            cp_async16(&sm.fv[buf][(s - nc) * SEG + 2 * k], sm.uf[s - nc].src + (size_t)ch * SEG + 2 * k);
+    }
+    cp_async_commit();
+}
+
 template <int VPL>
 __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
                                                    int nitems) {
-    constexpr int SEG = TileSmem<VPL>::SEG;
+    constexpr int SEG = UpdSmem<VPL>::SEG;
     extern __shared__ float4 smem_raw[];
-    TileSmem<VPL> &sm = *reinterpret_cast<TileSmem<VPL> *>(smem_raw);
+    UpdSmem<VPL> &sm = *reinterpret_cast<UpdSmem<VPL> *>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 item = items[it];
@@ -505,41 +534,42 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         const float2 *__restrict__ S = I.S[cur];
         float2 *__restrict__ Sn = I.S[cur ^ 1];
         const int NVp = I.NVp;
-        const float hdt = (float)I.hdt;
         const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
-        const int grad_on = I.gradient;
         const float4 *__restrict__ vt32 = I.vt32;
-        const float2 *__restrict__ bnd_out = I.bnd_out;
-        stage_common(I, tile, sm);
         const int j0 = I.cf_ptr[cs];
-        for (int c = threadIdx.x; c < nc; c += kT) sm.u.p2.ck[c] = I.ck[cs + c];
-        for (int c = threadIdx.x; c <= nc; c += kT) sm.u.p2.cf_off[c] = I.cf_ptr[cs + c] - j0;
+        for (int c = threadIdx.x; c < nc; c += kT) sm.ck[c] = I.ck[cs + c];
+        for (int c = threadIdx.x; c <= nc; c += kT) sm.cf_off[c] = I.cf_ptr[cs + c] - j0;
         const int ncf = I.cf_ptr[cs + nc] - j0;
-        for (int e = threadIdx.x; e < ncf; e += kT) sm.u.p2.cft[e] = I.cf_tf[j0 + e];
+        for (int e = threadIdx.x; e < ncf; e += kT) sm.cft[e] = I.cf_tf[j0 + e];
         const int q0 = I.tile_tf_ptr[tile], ntf = I.tile_tf_ptr[tile + 1] - q0;
         for (int q = threadIdx.x; q < ntf; q += kT) {
             const int f = I.tf_face[q0 + q];
-            TileFace x;
+            UpdFace x;
             x.n = I.fn32[f];
-            x.fdo = I.fdo[f];
-            x.fdn = I.fdn[f];
             x.area = I.farea[f];
             x.bnd = I.fbnd[f];
-            x.face = f;
-            x.os = I.tf_os[q0 + q];
-            x.ns = I.tf_ns[q0 + q];
+            x.src = x.bnd >= 0 ? I.bnd_out + (size_t)x.bnd * NVp : I.fbar + (size_t)f * NVp;
             if (x.bnd < 0) x.fk = I.fk[f];
-            sm.u.p2.tf[q] = x;
+            sm.uf[q] = x;
         }
-        for (int k = threadIdx.x; k < nc * 4; k += kT) sm.u.p2.acc[k] = 0.f;
+        for (int k = threadIdx.x; k < nc * 4; k += kT) sm.acc[k] = 0.f;
+        if (threadIdx.x == 0) {
+            sm.nc = nc;
+            sm.ntf = ntf;
+            sm.cs = cs;
+        }
         __syncthreads();
-        load_chunk<VPL>(S, NVp, ch0, 0, sm);
+        load_upd_chunk<VPL>(S, NVp, ch0, 0, sm);
         for (int ch = ch0; ch < ch1; ++ch) {
             const int buf = (ch - ch0) & 1;
-            next_chunk<VPL>(S, NVp, ch, ch1, buf, sm);
-            gradients(sm, buf, grad_on);
+            if (ch + 1 < ch1) {
+                load_upd_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
             __syncthreads();
-            float xx[VPL], xy[VPL], w[VPL], hx[VPL], hy[VPL], g0[VPL], x2[VPL];
+            float xx[VPL], xy[VPL], w[VPL], g0[VPL], x2[VPL];
             int p[VPL];
 #pragma unroll
             for (int v = 0; v < VPL; ++v) {
@@ -550,33 +580,29 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                 x2[v] = fmaf(xx[v], xx[v], xy[v] * xy[v]);
                 w[v] = t.z;
                 g0[v] = t.w;
-                hx[v] = hdt * xx[v];
-                hy[v] = hdt * xy[v];
             }
-            // each face touching a tile cell, once: its flux value (n0.xi) A f_face, seen from the owner
+            // each face touching a tile cell, once: its flux value (n0.xi) A f_face, seen from the owner;
+            // interior faces blend the stored reconstruction with the face equilibrium (:350-361)
             for (int q = warp; q < ntf; q += F32_WARPS) {
-                const TileFace &x = sm.u.p2.tf[q];
-                float2 *ff = sm.u.p2.ff + q * SEG + lane;
+                const UpdFace &x = sm.uf[q];
+                const float2 *fv = sm.fv[buf] + q * SEG + lane;
+                float2 *ff = sm.ff + q * SEG + lane;
                 const float2 n = x.n;
                 const float area = x.area;
                 if (x.bnd >= 0) {
-                    const float2 *bo = bnd_out + (size_t)x.bnd * NVp;
 #pragma unroll
                     for (int v = 0; v < VPL; ++v) {
                         const float knA = fmaf(n.x, xx[v], n.y * xy[v]) * area;
-                        const float2 gf = bo[p[v]];
+                        const float2 gf = fv[v * 32];
                         ff[v * 32] = make_float2(knA * gf.x, knA * gf.y);
                     }
                 } else {
                     const FaceK k = x.fk;
-                    const float2 fdo = x.fdo, fdn = x.fdn;
 #pragma unroll
                     for (int v = 0; v < VPL; ++v) {
-                        const float d = fmaf(n.x, xx[v], n.y * xy[v]);
-                        const int cls = classify(I, x.face, p[v], d, xx[v], xy[v]);
-                        const float2 gb = face_bar(sm, buf, v, cls, x.os, x.ns, fdo, fdn, hx[v], hy[v]);
+                        const float knA = fmaf(n.x, xx[v], n.y * xy[v]) * area;
+                        const float2 gb = fv[v * 32];
                         const float2 gs = dshakhov(k.e, xx[v], xy[v], x2[v], g0[v], k3, twoK);
-                        const float knA = d * area;
                         ff[v * 32] = make_float2(knA * fmaf(k.oCs, gb.x, k.Cs * gs.x), knA * fmaf(k.oCs, gb.y, k.Cs * gs.y));
                     }
                 }
@@ -586,10 +612,10 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                 float fg[VPL], fh[VPL];
 #pragma unroll
                 for (int v = 0; v < VPL; ++v) fg[v] = fh[v] = 0.f;
-                const int e1 = sm.u.p2.cf_off[cl + 1];
-                for (int e = sm.u.p2.cf_off[cl]; e < e1; ++e) {  // outward flux of the cell
-                    const unsigned char t = sm.u.p2.cft[e];
-                    const float2 *ff = sm.u.p2.ff + (t & 0x7f) * SEG + lane;
+                const int e1 = sm.cf_off[cl + 1];
+                for (int e = sm.cf_off[cl]; e < e1; ++e) {  // outward flux of the cell (:616-629)
+                    const unsigned char t = sm.cft[e];
+                    const float2 *ff = sm.ff + (t & 0x7f) * SEG + lane;
                     const float sgn = (t & 0x80) ? -1.f : 1.f;
 #pragma unroll
                     for (int v = 0; v < VPL; ++v) {
@@ -598,7 +624,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                         fh[v] = fmaf(sgn, val.y, fh[v]);
                     }
                 }
-                const CellK k = sm.u.p2.ck[cl];
+                const CellK k = sm.ck[cl];
                 float qv[2] = {0.f, 0.f};
 #pragma unroll
                 for (int v = 0; v < VPL; ++v) {
@@ -621,7 +647,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                 }
                 warp_sum(qv);
                 if (lane < 2) {
-                    float *a = sm.u.p2.acc + cl * 4 + 2 * lane;
+                    float *a = sm.acc + cl * 4 + 2 * lane;
                     kahan(a[0], a[1], lane == 0 ? qv[0] : qv[1]);
                 }
             }
@@ -630,7 +656,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         for (int k = threadIdx.x; k < nc * 2; k += kT) {
             const int cl = k >> 1, comp = k & 1;
             I.qpart[((size_t)grp * I.C + cs + cl) * 2 + comp] =
-                (double)sm.u.p2.acc[cl * 4 + 2 * comp] - (double)sm.u.p2.acc[cl * 4 + 2 * comp + 1];
+                (double)sm.acc[cl * 4 + 2 * comp] - (double)sm.acc[cl * 4 + 2 * comp + 1];
         }
         __syncthreads();
     }
@@ -1201,9 +1227,9 @@ int fp32_configure(int device) {
     (void)device;
     const int a1 = (int)tile_smem<1>(), a2 = (int)tile_smem<2>();
     if (cudaFuncSetAttribute(k32_moments<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, a1) != cudaSuccess ||
-        cudaFuncSetAttribute(k32_update<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, a1) != cudaSuccess ||
+        cudaFuncSetAttribute(k32_update<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<1>()) != cudaSuccess ||
         cudaFuncSetAttribute(k32_moments<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, a2) != cudaSuccess ||
-        cudaFuncSetAttribute(k32_update<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, a2) != cudaSuccess)
+        cudaFuncSetAttribute(k32_update<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<2>()) != cudaSuccess)
         return -1;
     return 0;
 }
@@ -1220,12 +1246,12 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     int n = 0;
     auto tiles = [&](bool update) {
         if (n2 > 0) {
-            if (update) k32_update<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
+            if (update) k32_update<2><<<grid2, kT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
             else k32_moments<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
             ++n;
         }
         if (n1 > 0) {
-            if (update) k32_update<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
+            if (update) k32_update<1><<<grid1, kT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
             else k32_moments<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
             ++n;
         }

@@ -99,6 +99,7 @@ struct F32Inst {
     double *fgbar;         // [F][4] fluxes of the reconstructed values (mass, mom x, mom y, energy) per unit area along n0
     double *fsum;          // [F][4] same for the face equilibrium (interior) or the final boundary values
     float2 *bnd_in, *bnd_out;  // [nb][NVp]
+    float2 *fbar;              // [F][NVp] reconstructed interior face values (moments -> update kernel)
     double *bnd_g0;            // [nb][2] half-range sums of g0 (fp32_prepare)
     CellK *ck;             // [C]
     double *qpart;         // [ngroup][C][2]

@@ -49,16 +49,17 @@ struct Request {
     }
 };
 
-// Device bytes of an FP32 solve: two state buffers, boundary face buffers,
+// Device bytes of an FP32 solve: two state buffers, the stored face values, boundary face buffers,
 // per-face and per-cell work arrays and the geometry tables.
 size_t estimate_bytes(const meso_mesh_desc &m, const meso_dvs_desc &d) {
     const size_t NVp = ((size_t)d.nv + 63) / 64 * 64;
     const size_t C = m.ncell, F = m.nface;
     const size_t nb = 4 * (size_t)std::sqrt((double)C) + 64;  // boundary faces of a 2-D domain, with margin
     const size_t state = 2 * C * NVp * 8;
+    const size_t faces = F * NVp * 8;  // stored face reconstructions
     const size_t bnd = 2 * nb * NVp * 8;
     const size_t work = F * (8 * 11 * 4 + 200) + C * 400;  // face partials (up to 4 groups), tables
-    return state + bnd + work + ((size_t)16 << 20);
+    return state + faces + bnd + work + ((size_t)16 << 20);
 }
 
 }  // namespace
