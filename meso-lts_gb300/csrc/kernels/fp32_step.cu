@@ -206,13 +206,6 @@ struct OwnedFace {     // P1: one face owned by the tile
     unsigned short os, ns;
     int pad;
 };
-struct UpdFace {       // P2: one face touching a tile cell (evaluated once per chunk)
-    FaceK fk;
-    const float2 *src;  // its reconstructed (interior) or final (boundary) values, [NVp]
-    float2 n;
-    float area;
-    int bnd;
-};
 
 template <int VPL> struct __align__(128) TileSmem {
     static constexpr int SEG = 32 * VPL;         // velocities of one slot in a chunk
@@ -240,10 +233,9 @@ template <int VPL> constexpr size_t tile_smem() { return sizeof(TileSmem<VPL>); 
 template <int VPL> struct __align__(128) UpdSmem {
     static constexpr int SEG = 32 * VPL;
     float2 phi[2][F32_MAX_CELLS * SEG];         // tile cells (cp.async target)
-    float2 fv[2][F32_MAX_TF * SEG];             // face values (cp.async target)
-    float2 ff[F32_MAX_TF * SEG];                // (n0.xi) A f_face of each tile face, this chunk
+    float2 fv[2][F32_MAX_TF * SEG];             // (n0.xi) A f_face of each tile face (cp.async target)
+    const float2 *src[F32_MAX_TF];              // where each tile face's flux values are, [NVp]
     CellK ck[F32_MAX_CELLS];
-    UpdFace uf[F32_MAX_TF];
     int cf_off[F32_MAX_CELLS + 1];
     float acc[F32_MAX_CELLS * 4];
     unsigned char cft[F32_MAX_CF];              // per cell-face entry: tile face | 0x80 if the cell is its neighbour
@@ -509,7 +501,7 @@ __device__ __forceinline__ void load_upd_chunk(const float2 *S, int NVp, int ch,
         if (s < nc)
             cp_async16(&sm.phi[buf][s * SEG + 2 * k], S + (size_t)(sm.cs + s) * NVp + (size_t)ch * SEG + 2 * k);
         else
-            cp_async16(&sm.fv[buf][(s - nc) * SEG + 2 * k], sm.uf[s - nc].src + (size_t)ch * SEG + 2 * k);
+            cp_async16(&sm.fv[buf][(s - nc) * SEG + 2 * k], sm.src[s - nc] + (size_t)ch * SEG + 2 * k);
     }
     cp_async_commit();
 }
@@ -543,14 +535,8 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         for (int e = threadIdx.x; e < ncf; e += kT) sm.cft[e] = I.cf_tf[j0 + e];
         const int q0 = I.tile_tf_ptr[tile], ntf = I.tile_tf_ptr[tile + 1] - q0;
         for (int q = threadIdx.x; q < ntf; q += kT) {
-            const int f = I.tf_face[q0 + q];
-            UpdFace x;
-            x.n = I.fn32[f];
-            x.area = I.farea[f];
-            x.bnd = I.fbnd[f];
-            x.src = x.bnd >= 0 ? I.bnd_out + (size_t)x.bnd * NVp : I.fbar + (size_t)f * NVp;
-            if (x.bnd < 0) x.fk = I.fk[f];
-            sm.uf[q] = x;
+            const int f = I.tf_face[q0 + q], b = I.fbnd[f];
+            sm.src[q] = b >= 0 ? I.bnd_out + (size_t)b * NVp : I.fbar + (size_t)f * NVp;
         }
         for (int k = threadIdx.x; k < nc * 4; k += kT) sm.acc[k] = 0.f;
         if (threadIdx.x == 0) {
@@ -581,33 +567,6 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                 w[v] = t.z;
                 g0[v] = t.w;
             }
-            // each face touching a tile cell, once: its flux value (n0.xi) A f_face, seen from the owner;
-            // interior faces blend the stored reconstruction with the face equilibrium (:350-361)
-            for (int q = warp; q < ntf; q += F32_WARPS) {
-                const UpdFace &x = sm.uf[q];
-                const float2 *fv = sm.fv[buf] + q * SEG + lane;
-                float2 *ff = sm.ff + q * SEG + lane;
-                const float2 n = x.n;
-                const float area = x.area;
-                if (x.bnd >= 0) {
-#pragma unroll
-                    for (int v = 0; v < VPL; ++v) {
-                        const float knA = fmaf(n.x, xx[v], n.y * xy[v]) * area;
-                        const float2 gf = fv[v * 32];
-                        ff[v * 32] = make_float2(knA * gf.x, knA * gf.y);
-                    }
-                } else {
-                    const FaceK k = x.fk;
-#pragma unroll
-                    for (int v = 0; v < VPL; ++v) {
-                        const float knA = fmaf(n.x, xx[v], n.y * xy[v]) * area;
-                        const float2 gb = fv[v * 32];
-                        const float2 gs = dshakhov(k.e, xx[v], xy[v], x2[v], g0[v], k3, twoK);
-                        ff[v * 32] = make_float2(knA * fmaf(k.oCs, gb.x, k.Cs * gs.x), knA * fmaf(k.oCs, gb.y, k.Cs * gs.y));
-                    }
-                }
-            }
-            __syncthreads();
             for (int cl = warp; cl < nc; cl += F32_WARPS) {
                 float fg[VPL], fh[VPL];
 #pragma unroll
@@ -615,7 +574,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                 const int e1 = sm.cf_off[cl + 1];
                 for (int e = sm.cf_off[cl]; e < e1; ++e) {  // outward flux of the cell (:616-629)
                     const unsigned char t = sm.cft[e];
-                    const float2 *ff = sm.ff + (t & 0x7f) * SEG + lane;
+                    const float2 *ff = sm.fv[buf] + (t & 0x7f) * SEG + lane;
                     const float sgn = (t & 0x80) ? -1.f : 1.f;
 #pragma unroll
                     for (int v = 0; v < VPL; ++v) {
@@ -743,20 +702,39 @@ __global__ void __launch_bounds__(256) k32_face_eqflux(const F32Inst *__restrict
         if (I.fbnd[f] >= 0) continue;
         const FaceK k = I.fk[f];
         const float2 n = I.fn32[f];
+        const float area = I.farea[f];
         const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
         const float4 *__restrict__ vt32 = I.vt32;
-        // plain FP32 sums over blocks of 8 velocities per lane, compensated across blocks
+        float2 *__restrict__ fb = I.fbar + (size_t)f * I.NVp;
+        // plain FP32 sums over blocks of 8 velocities per lane, compensated across blocks; each
+        // block's table entries and stored reconstructions are loaded before any is used
         float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
         for (int p0 = 0; p0 < I.NVp; p0 += 32 * 8) {
             float b[4] = {0.f, 0.f, 0.f, 0.f};
-            const int pe = min(I.NVp, p0 + 32 * 8);
-#pragma unroll 2
-            for (int p = p0 + lane; p < pe; p += 32) {
-                const float4 t = vt32[p];
+            float4 tv[8];
+            float2 gv[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int p = p0 + 32 * i + lane;
+                if (p < I.NVp) {
+                    tv[i] = vt32[p];
+                    gv[i] = fb[p];
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int p = p0 + 32 * i + lane;
+                if (p >= I.NVp) continue;
+                const float4 t = tv[i];
                 const float xx = t.x, xy = t.y, w = t.z;
                 const float x2 = fmaf(xx, xx, xy * xy);
                 const float2 gs = dshakhov(k.e, xx, xy, x2, t.w, k3, twoK);
-                const float wkn = w * fmaf(n.x, xx, n.y * xy);
+                // the face's flux value (n0.xi) A (blend of the reconstruction and the equilibrium,
+                // cdugks_shakhov.cpp:350-361), in place of the reconstruction, for the update kernel
+                const float2 gb = gv[i];
+                const float d = fmaf(n.x, xx, n.y * xy), knA = d * area;
+                fb[p] = make_float2(knA * fmaf(k.oCs, gb.x, k.Cs * gs.x), knA * fmaf(k.oCs, gb.y, k.Cs * gs.y));
+                const float wkn = w * d;
                 const float a = wkn * gs.x;
                 b[0] += a;
                 b[1] = fmaf(a, xx, b[1]);
@@ -933,7 +911,9 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
                     }
                 }
             }
-            bout[p] = v;
+            // the face's flux value (n0.xi) A f for the update kernel
+            const float knA = d * I.farea[f];
+            bout[p] = make_float2(knA * v.x, knA * v.y);
             // moment fluxes of the deviations along n0 (the g0 parts are added in FP64 below)
             const float wkn = w * d;
             const float a = wkn * v.x;
