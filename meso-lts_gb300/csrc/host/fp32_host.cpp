@@ -185,9 +185,9 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         const size_t cv = (size_t)C * NVp;
         I.S[0] = A.alloc<float2>(cv);
         I.S[1] = A.alloc<float2>(cv);
-        I.fpart = A.alloc<double>((size_t)I.ngroup * F * meso::F32_NMOM);
         I.u32 = A.alloc<float2>(C);
         I.fk = A.alloc<meso::FaceK>(F);
+        I.fmom = A.alloc<double>((size_t)F * meso::F32_NMOM);
         I.fmac = A.alloc<double>((size_t)F * 8);
         I.fgbar = A.alloc<double>((size_t)F * 4);
         I.fsum = A.alloc<double>((size_t)F * 4);

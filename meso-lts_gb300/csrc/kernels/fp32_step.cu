@@ -5,39 +5,47 @@
 // VPL (velocities per lane) is 2 for velocity sets of 256 and more, 1 below:
 // a chunk is 32 VPL velocities, lane l of a warp handles velocities
 // chunk*32*VPL + v*32 + l, v < VPL.
-// A step is seven launches, each over all instances of a batch:
+// A step is ten launches, each over all instances of a batch, replayed as one
+// CUDA graph:
 //
-//   P1  k32_moments      per (tile, velocity group) CTA: stage the tile and its
-//                        two-ring halo for one chunk in shared memory,
-//                        compute every tile / 1-ring cell's least-squares
-//                        gradient once, reconstruct each owned face (half-step
-//                        upwind, cdugks_shakhov.cpp:223-276) and accumulate 11
-//                        raw moments about a reference velocity (FP32 terms,
-//                        warp sums, compensated FP32 across chunks, FP64
-//                        partial per group)
-//   FMa k32_face_macros  one thread per face, FP64: face rho, u, T, tau, q
+//   P1  k32_reconstruct  per (tile, velocity group) CTA: the tile and its
+//                        two-ring halo of one chunk of 32 VPL velocities
+//                        double-buffered in shared memory (16-byte cp.async
+//                        copies by all threads), least-squares gradients of the
+//                        tile and 1-ring cells once per chunk, and the half-step
+//                        upwind reconstruction of each face the tile owns
+//                        (cdugks_shakhov.cpp:223-276) stored to HBM (fbar, or
+//                        bnd_in for boundary faces)
+//   FMa k32_face_moments one warp per face: 11 raw moments about a reference
+//                        velocity of the stored reconstruction (FP32 terms,
+//                        compensated, FP64 warp sum)
+//       k32_face_macros  one thread per face, FP64: face rho, u, T, tau, q
 //                        (cdugks_shakhov.cpp:341-349) and the moment fluxes of
-//                        the reconstructed values, by exact algebra on the moments
+//                        the reconstruction, by exact algebra on the moments
 //   FMb k32_face_eqflux  one warp per interior face: discrete moment fluxes of
-//                        the face Shakhov equilibrium (FP32 terms, FP64 result)
+//                        the face Shakhov equilibrium (FP32 terms, FP64 result),
+//                        and the face's flux value (n0.xi) A (blend of the
+//                        reconstruction and the equilibrium) stored in place
 //   BND k32_boundary     one block per boundary face: blend, diffuse-wall
 //                        balance, inlets / outlets, symmetry, slip
-//                        (cdugks_shakhov.cpp:364-607), moment fluxes
+//                        (cdugks_shakhov.cpp:364-607), moment fluxes, flux values
 //   CM  k32_cell_macros  one thread per cell, FP64: flux moments from the face
 //                        fluxes, conservative update, tau, evolution constants
 //                        (cdugks_shakhov.cpp:636-668), NaN / T<0 monitor
-//   P2  k32_update       per (tile, group) CTA: same staging and gradients, then
-//                        per cell and velocity: face values (reconstruction
-//                        blended with the face equilibrium, or the boundary
-//                        value), flux, evolution to f-bar-plus, heat-flux
-//                        partials (cdugks_shakhov.cpp:616-696)
-//   QR  k32_heat_flux    q = sum of the heat-flux partials (FP64)
+//   P2  k32_update       per (tile, group) CTA: the tile's cells and the flux
+//                        values of every face touching them, one chunk at a
+//                        time; per cell and velocity the signed sum of its faces'
+//                        flux values, evolution to f-bar-plus, heat-flux partials
+//                        (cdugks_shakhov.cpp:616-696)
+//   QR  k32_heat_flux    q = sum of the heat-flux partials (FP64); then the mask
+//                        repair and the end-of-step counter
 //
-// Face values never go to HBM except on boundary faces: the state is read
-// twice and written once per step.  Upwind classification is exact: n.xi is
-// evaluated in FP32 and re-evaluated in FP64 in the reference's order when it
-// lies within a rounding margin of zero.  Per-face and per-cell scalar work
-// (pow, divisions) runs one thread per face / cell in FP64.
+// The state is read twice and written once per step; each face's values are
+// written once (reconstruction), read and rewritten once (flux value) and read
+// by the one or two tiles whose cells it bounds.  Upwind classification is
+// exact: n.xi is evaluated in FP32 and re-evaluated in FP64 in the reference's
+// order when it lies within a rounding margin of zero.  Per-face and per-cell
+// scalar work (pow, divisions) runs one thread per face / cell in FP64.
 #include <cfloat>
 #include <cstddef>
 #include <climits>
@@ -123,7 +131,7 @@ __device__ __forceinline__ EqP make_eqp(const F32Inst &I, double rho, double ux,
 }
 
 // The 11 raw moments of the reference pair about velocity (a, b), from the discrete
-// moments of g0 (same order as the moments k32_moments accumulates).
+// moments of g0 (same order as the moments k32_face_macros accumulates).
 __device__ __forceinline__ void g0_raw_moments(const F32Inst &I, double a, double b, double (&M)[F32_NMOM]) {
     const double *G = I.gmom;  // 1, x, y, xx, xy, yy, xxx, xxy, xyy, yyy
     const double g1 = G[0], gx = G[1], gy = G[2], gxx = G[3], gxy = G[4], gyy = G[5];
@@ -201,7 +209,7 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
 }
 
 struct OwnedFace {     // P1: one face owned by the tile
-    float2 n, fdo, fdn, u0;
+    float2 n, fdo, fdn;
     int bnd, face;
     unsigned short os, ns;
     int pad;
@@ -219,7 +227,6 @@ template <int VPL> struct __align__(128) TileSmem {
     union {
         struct {
             OwnedFace of[F32_MAX_OWNED];
-            float acc[F32_MAX_OWNED * 22];
         } p1;
 
     } u;
@@ -350,43 +357,12 @@ __device__ __forceinline__ float2 face_bar(const TileSmem<VPL> &sm, int buf, int
     return make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
 }
 
-// Sum of 16 values over the warp by halving exchanges: lane l ends with the total of value l >> 1.
-__device__ __forceinline__ float warp_sum16(float (&v)[16], int lane) {
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const bool up = lane & 16;
-        const float send = up ? v[k] : v[k + 8];
-        const float keep = up ? v[k + 8] : v[k];
-        v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-    }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const bool up = lane & 8;
-        const float send = up ? v[k] : v[k + 4];
-        const float keep = up ? v[k + 4] : v[k];
-        v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-    }
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const bool up = lane & 4;
-        const float send = up ? v[k] : v[k + 2];
-        const float keep = up ? v[k + 2] : v[k];
-        v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-    }
-    {
-        const bool up = lane & 2;
-        const float send = up ? v[0] : v[1];
-        const float keep = up ? v[1] : v[0];
-        v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
-    }
-    return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
-}
 
 // =============================================================================
-// P1: raw face moments
+// P1: upwind half-step reconstruction of every face (owned by a tile) into HBM
 // =============================================================================
 template <int VPL>
-__global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
+__global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
                                                     int nitems) {
     constexpr int SEG = TileSmem<VPL>::SEG;
     extern __shared__ float4 smem_raw[];
@@ -416,8 +392,6 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
             o.n = I.fn32[g];
             o.fdo = I.fdo[g];
             o.fdn = I.fdn[g];
-            const float2 uo = I.u32[I.fown[g]], un = I.u32[I.fnei[g]];
-            o.u0 = make_float2(0.5f * (uo.x + un.x), 0.5f * (uo.y + un.y));
             o.bnd = I.fbnd[g];
             o.face = g;
             o.os = I.face_own_slot[g];
@@ -425,7 +399,6 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
             o.pad = 0;
             sm.u.p1.of[f] = o;
         }
-        for (int k = threadIdx.x; k < nOF * 22; k += kT) sm.u.p1.acc[k] = 0.f;
         __syncthreads();
         load_chunk<VPL>(S, NVp, ch0, 0, sm);
         for (int ch = ch0; ch < ch1; ++ch) {
@@ -433,7 +406,7 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
             next_chunk<VPL>(S, NVp, ch, ch1, buf, sm);
             gradients(sm, buf, grad_on);
             __syncthreads();
-            float xx[VPL], xy[VPL], w[VPL], hx[VPL], hy[VPL];
+            float xx[VPL], xy[VPL], hx[VPL], hy[VPL];
             int p[VPL];
 #pragma unroll
             for (int v = 0; v < VPL; ++v) {
@@ -441,49 +414,20 @@ __global__ void __launch_bounds__(kT, 1) k32_moments(const F32Inst *__restrict__
                 const float4 t = vt32[p[v]];
                 xx[v] = t.x;
                 xy[v] = t.y;
-                w[v] = t.z;
                 hx[v] = hdt * xx[v];
                 hy[v] = hdt * xy[v];
             }
             for (int fl = warp; fl < nOF; fl += F32_WARPS) {
                 const OwnedFace o = sm.u.p1.of[fl];
-                float m[16];
-#pragma unroll
-                for (int k = 0; k < 16; ++k) m[k] = 0.f;
+                float2 *dst = o.bnd >= 0 ? bnd_in + (size_t)o.bnd * NVp : fbar + (size_t)o.face * NVp;
 #pragma unroll
                 for (int v = 0; v < VPL; ++v) {
                     const int cls = classify(I, o.face, p[v], fmaf(o.n.x, xx[v], o.n.y * xy[v]), xx[v], xy[v]);
-                    const float2 gb = face_bar(sm, buf, v, cls, o.os, o.ns, o.fdo, o.fdn, hx[v], hy[v]);
-                    if (o.bnd >= 0) bnd_in[(size_t)o.bnd * NVp + p[v]] = gb;
-                    else fbar[(size_t)o.face * NVp + p[v]] = gb;  // read by the update kernel
-                    const float c0x = xx[v] - o.u0.x, c0y = xy[v] - o.u0.y;
-                    const float wg = w[v] * gb.x, wh = w[v] * gb.y;
-                    const float cc = fmaf(c0x, c0x, c0y * c0y);
-                    const float a = c0x * wg, b = c0y * wg;
-                    m[0] += wg;
-                    m[1] += a;
-                    m[2] += b;
-                    m[3] = fmaf(c0x, a, m[3]);
-                    m[4] = fmaf(c0x, b, m[4]);
-                    m[5] = fmaf(c0y, b, m[5]);
-                    m[6] = fmaf(cc, a, m[6]);
-                    m[7] = fmaf(cc, b, m[7]);
-                    m[8] += wh;
-                    m[9] = fmaf(c0x, wh, m[9]);
-                    m[10] = fmaf(c0y, wh, m[10]);
-                }
-                const float tot = warp_sum16(m, lane);
-                if ((lane & 1) == 0 && (lane >> 1) < F32_NMOM) {
-                    float *acc = sm.u.p1.acc + fl * 22 + 2 * (lane >> 1);
-                    kahan(acc[0], acc[1], tot);
+                    dst[p[v]] = face_bar(sm, buf, v, cls, o.os, o.ns, o.fdo, o.fdn, hx[v], hy[v]);
                 }
             }
             __syncthreads();
         }
-        double *out = I.fpart + ((size_t)grp * I.F + fs) * F32_NMOM;
-        for (int k = threadIdx.x; k < nOF * F32_NMOM; k += kT)
-            out[k] = (double)sm.u.p1.acc[2 * k] - (double)sm.u.p1.acc[2 * k + 1];
-        __syncthreads();
     }
 }
 
@@ -622,8 +566,79 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
 }
 
 // =============================================================================
-// FMa: face macros from the raw moments (one thread per face, FP64)
+// FMa: face moments from the stored reconstructions (one warp per face), face macros in FP64
 // =============================================================================
+__global__ void __launch_bounds__(256) k32_face_moments(const F32Inst *__restrict__ insts, const int *__restrict__ foff,
+                                                       int ninst, int total) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
+        const int i = find_inst(foff, ninst, g);
+        const F32Inst &I = insts[i];
+        if (step_stopped(I.status)) continue;
+        const int f = g - foff[i];
+        const float2 uo = I.u32[I.fown[f]], un = I.u32[I.fnei[f]];
+        const float u0xf = 0.5f * (uo.x + un.x), u0yf = 0.5f * (uo.y + un.y);
+        // 11 raw moments about u0 of the face's reconstructed deviations (cdugks_shakhov.cpp:305-349):
+        // FP32 terms summed over blocks of 4 velocities per lane, compensated across blocks
+        const int b = I.fbnd[f];
+        const float2 *__restrict__ src = b >= 0 ? I.bnd_in + (size_t)b * I.NVp : I.fbar + (size_t)f * I.NVp;
+        const float4 *__restrict__ vt32 = I.vt32;
+        float s[F32_NMOM], c[F32_NMOM];
+#pragma unroll
+        for (int k = 0; k < F32_NMOM; ++k) s[k] = c[k] = 0.f;
+        for (int p0 = 0; p0 < I.NVp; p0 += 32 * 4) {
+            float4 tv[4];
+            float2 gv[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int p = p0 + 32 * j + lane;
+                tv[j] = p < I.NVp ? vt32[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+                gv[j] = p < I.NVp ? src[p] : make_float2(0.f, 0.f);
+            }
+            float m[F32_NMOM];
+#pragma unroll
+            for (int k = 0; k < F32_NMOM; ++k) m[k] = 0.f;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float c0x = tv[j].x - u0xf, c0y = tv[j].y - u0yf;
+                const float wg = tv[j].z * gv[j].x, wh = tv[j].z * gv[j].y;
+                const float cc = fmaf(c0x, c0x, c0y * c0y);
+                const float a = c0x * wg, bb = c0y * wg;
+                m[0] += wg;
+                m[1] += a;
+                m[2] += bb;
+                m[3] = fmaf(c0x, a, m[3]);
+                m[4] = fmaf(c0x, bb, m[4]);
+                m[5] = fmaf(c0y, bb, m[5]);
+                m[6] = fmaf(cc, a, m[6]);
+                m[7] = fmaf(cc, bb, m[7]);
+                m[8] += wh;
+                m[9] = fmaf(c0x, wh, m[9]);
+                m[10] = fmaf(c0y, wh, m[10]);
+            }
+#pragma unroll
+            for (int k = 0; k < F32_NMOM; ++k) kahan(s[k], c[k], m[k]);
+        }
+        double M[F32_NMOM];
+#pragma unroll
+        for (int k = 0; k < F32_NMOM; ++k) {
+            double v = (double)s[k] - (double)c[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            M[k] = v;
+        }
+        if (lane < F32_NMOM) {
+            double mine = M[0];
+#pragma unroll
+            for (int k = 1; k < F32_NMOM; ++k)
+                if (lane == k) mine = M[k];
+            I.fmom[(size_t)f * F32_NMOM + lane] = mine;
+        }
+    }
+}
+
+// FP64 face macros from the moments (one thread per face)
 __global__ void k32_face_macros(const F32Inst *__restrict__ insts, const int *__restrict__ foff, int ninst,
                                 int total) {
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
@@ -631,14 +646,10 @@ __global__ void k32_face_macros(const F32Inst *__restrict__ insts, const int *__
         const F32Inst &I = insts[i];
         if (step_stopped(I.status)) continue;
         const int f = g - foff[i];
-        double M[F32_NMOM];
-        for (int k = 0; k < F32_NMOM; ++k) M[k] = 0.0;
-        for (int grp = 0; grp < I.ngroup; ++grp) {
-            const double *pp = I.fpart + ((size_t)grp * I.F + f) * F32_NMOM;
-            for (int k = 0; k < F32_NMOM; ++k) M[k] += pp[k];
-        }
         const float2 uo = I.u32[I.fown[f]], un = I.u32[I.fnei[f]];
         const double u0x = (double)(0.5f * (uo.x + un.x)), u0y = (double)(0.5f * (uo.y + un.y));
+        double M[F32_NMOM];
+        for (int k = 0; k < F32_NMOM; ++k) M[k] = I.fmom[(size_t)f * F32_NMOM + k];
         {  // the reference pair's part of the moments, exactly in FP64
             double M0[F32_NMOM];
             g0_raw_moments(I, u0x, u0y, M0);
@@ -1206,15 +1217,15 @@ int grid_of(int total, int per_block, int cap) {
 int fp32_configure(int device) {
     (void)device;
     const int a1 = (int)tile_smem<1>(), a2 = (int)tile_smem<2>();
-    if (cudaFuncSetAttribute(k32_moments<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, a1) != cudaSuccess ||
+    if (cudaFuncSetAttribute(k32_reconstruct<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, a1) != cudaSuccess ||
         cudaFuncSetAttribute(k32_update<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<1>()) != cudaSuccess ||
-        cudaFuncSetAttribute(k32_moments<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, a2) != cudaSuccess ||
+        cudaFuncSetAttribute(k32_reconstruct<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, a2) != cudaSuccess ||
         cudaFuncSetAttribute(k32_update<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<2>()) != cudaSuccess)
         return -1;
     return 0;
 }
 
-const char *const kFp32Phases[] = {"k32_moments", "k32_face_macros", "k32_face_eqflux", "k32_boundary",
+const char *const kFp32Phases[] = {"k32_reconstruct", "k32_face_moments+macros", "k32_face_eqflux", "k32_boundary",
                                    "k32_cell_macros", "k32_update", "k32_heat_flux+repair+end"};
 
 int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev) {
@@ -1227,12 +1238,12 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     auto tiles = [&](bool update) {
         if (n2 > 0) {
             if (update) k32_update<2><<<grid2, kT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
-            else k32_moments<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
+            else k32_reconstruct<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
             ++n;
         }
         if (n1 > 0) {
             if (update) k32_update<1><<<grid1, kT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
-            else k32_moments<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
+            else k32_reconstruct<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
             ++n;
         }
     };
@@ -1242,13 +1253,15 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     mark(0);
     tiles(false);
     mark(1);
+    k32_face_moments<<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
+                                                                         s.total_faces);
     k32_face_macros<<<grid_of(s.total_faces, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
                                                                           s.total_faces);
     mark(2);
     k32_face_eqflux<<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
                                                                         s.total_faces);
     mark(3);
-    n += 2;
+    n += 3;
     if (s.total_bnd > 0) {
         k32_boundary<<<grid_of(s.total_bnd, 1, cap), 256, 0, stream>>>(s.d_inst, s.d_bnd_items, s.ninst, s.total_bnd);
         ++n;

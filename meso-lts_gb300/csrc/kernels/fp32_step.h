@@ -92,9 +92,9 @@ struct F32Inst {
     const int *sym;
     // state and work buffers
     float2 *S[2];          // [C][NVp] (g - g0, h - h0) ping-pong; S[status->step & 1] is current
-    double *fpart;         // [ngroup][F][11] raw face-moment partials
     float2 *u32;           // [C] cell velocity (FP32) = reference velocity of the face moments
     FaceK *fk;             // [F]
+    double *fmom;          // [F][11] raw face moments of the reconstruction (deviation part)
     double *fmac;          // [F][8] rho, ux, uy, T, qx, qy, Cs, tau
     double *fgbar;         // [F][4] fluxes of the reconstructed values (mass, mom x, mom y, energy) per unit area along n0
     double *fsum;          // [F][4] same for the face equilibrium (interior) or the final boundary values
