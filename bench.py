@@ -166,14 +166,15 @@ def measured_peak_hbm() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def ncu_traffic() -> float | None:
+def ncu_traffic() -> tuple[float | None, str | None]:
     """DRAM bytes per k32_update launch from the committed ncu summary (profiles/), if present."""
     p = os.path.join(ROOT, "profiles", "k32_update_config2.json")
     try:
         with open(p) as f:
-            return float(json.load(f)["dram_bytes_per_launch"])
+            d = json.load(f)
+        return float(d["dram_bytes_per_launch"]), d.get("traffic_note")
     except (OSError, KeyError, ValueError):
-        return None
+        return None, None
 
 
 def build_workload(tmp: str, precision: str) -> str:
@@ -477,7 +478,7 @@ def main() -> int:
         upd_ms = phases.get("k32_update", None)
         alg_bytes = 16.0 * cx
         achieved = alg_bytes / (upd_ms * 1e-3) / 1e9 if upd_ms else None
-        traffic = ncu_traffic()
+        traffic, traffic_note = ncu_traffic()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -491,7 +492,9 @@ def main() -> int:
             "phases_ms": phases,
             "roofline": {"bound": "hbm", "kernel": "k32_update", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak if achieved else None,
-                         "traffic": traffic, "alg_bytes_per_launch": alg_bytes},
+                         "traffic": traffic, "alg_bytes_per_launch": alg_bytes, "traffic_note": traffic_note,
+                         "step_achieved": alg_bytes / (ms_max / K * 1e-3) / 1e9,
+                         "step_note": "whole step: state bytes (16 B per cell-velocity) over the step time"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "note": "initial fields host->device once per K steps; macros device->host every step"},
             "clocks": clk.summary(),
