@@ -156,11 +156,26 @@ bool build_tile_plan(const meso_mesh_desc &m, const Renumbering &rn, const std::
                 }
         }
         std::sort(l1.begin(), l1.end());
-        for (int x : l1) {
+        // 1-ring cells that are the neighbour of a face the tile owns are reconstructed from, so they
+        // need a gradient (and their own neighbours); the rest are only neighbours of tile cells
+        std::vector<int> l1a, l1b;
+        {
+            std::vector<char> up(l1.size(), 0);
+            for (int f = fcur; f < F && fown[f] < cs + n; ++f) {
+                auto it = std::lower_bound(l1.begin(), l1.end(), fnei[f]);
+                if (it != l1.end() && *it == fnei[f]) up[it - l1.begin()] = 1;
+            }
+            for (size_t k = 0; k < l1.size(); ++k) (up[k] ? l1a : l1b).push_back(l1[k]);
+        }
+        for (int x : l1a) {
             slot_of[x] = (int)slots.size();
             slots.push_back(x);
         }
-        for (int c : l1) {
+        for (int x : l1b) {
+            slot_of[x] = (int)slots.size();
+            slots.push_back(x);
+        }
+        for (int c : l1a) {
             nbrs(c, nb);
             for (int x : nb)
                 if (stamp[x] != t) {
@@ -173,7 +188,7 @@ bool build_tile_plan(const meso_mesh_desc &m, const Renumbering &rn, const std::
             slot_of[x] = (int)slots.size();
             slots.push_back(x);
         }
-        const int ng = n + (int)l1.size();
+        const int ng = n + (int)l1a.size();
         P.tile_gslots.push_back(ng);
         P.slot_cell.insert(P.slot_cell.end(), slots.begin(), slots.end());
         // gradient stencils of tile + 1-ring slots
