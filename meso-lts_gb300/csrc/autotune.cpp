@@ -34,7 +34,7 @@ std::map<std::tuple<int, int, int>, Shape> g_cache;  // (cells, faces, velocitie
 std::vector<Shape> candidates(int nv, int ncell, int num_sms) {
     std::vector<Shape> out;
     const int vmax = nv >= 64 ? 2 : 1;
-    for (int T : {16, 24, 32})
+    for (int T : {24, 32, 40, 48})
         for (int v = 1; v <= vmax; ++v) {
             out.push_back({T, v, 0});
             // more velocity groups when the mesh has few tiles for the SM count

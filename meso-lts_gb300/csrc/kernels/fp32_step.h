@@ -16,14 +16,14 @@ namespace meso {
 // Kernel limits (the tile planner shrinks tiles until every tile fits).
 constexpr int F32_WARPS = 16;       // warps per CTA of the tile kernels
 constexpr int F32_MAX_VPL = 2;      // velocities per lane (a chunk is 32 x VPL velocities)
-constexpr int F32_MAX_SLOTS = 92;   // tile + two-ring halo cells
-constexpr int F32_MAX_GSLOTS = 64;  // tile + one-ring halo cells (gradients)
-constexpr int F32_MAX_GENT = 352;   // gradient stencil entries per tile
-constexpr int F32_MAX_OWNED = 84;   // faces owned by a tile
-constexpr int F32_MAX_CELLS = 32;   // cells per tile
-constexpr int F32_DEFAULT_CELLS = 32;  // tile size without an autotuned shape (two cells per warp)
-constexpr int F32_MAX_CF = 132;     // cell-face entries per tile (tile cells x faces per cell)
-constexpr int F32_MAX_TF = 84;      // faces touching a tile cell (< 128: indices fit 7 bits)
+constexpr int F32_MAX_SLOTS = 104;  // tile + 1-ring + (part of the) 2-ring halo cells
+constexpr int F32_MAX_GSLOTS = 72;  // slots with a gradient (tile + 1-ring cells owned faces reconstruct from)
+constexpr int F32_MAX_GENT = 400;   // gradient stencil entries per tile
+constexpr int F32_MAX_OWNED = 112;  // faces owned by a tile
+constexpr int F32_MAX_CELLS = 48;   // cells per tile
+constexpr int F32_DEFAULT_CELLS = 48;  // tile size without an autotuned shape (three cells per warp)
+constexpr int F32_MAX_CF = 200;     // cell-face entries per tile (tile cells x faces per cell)
+constexpr int F32_MAX_TF = 120;     // faces touching a tile cell (< 128: indices fit 7 bits)
 constexpr int F32_NMOM = 11;        // raw face moments about the reference velocity (2-D)
 
 // Scalars of one Shakhov equilibrium (rho, u, T, q) for FP32 evaluation of its

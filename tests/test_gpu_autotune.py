@@ -15,7 +15,7 @@ def test_autotune_picks_and_remembers_a_shape(gpu, tmp_path):
     try:
         best, ms = mg.autotune(path, steps=3)
         assert ms > 0.0
-        assert best.tile_cells in (16, 24, 32) and best.vpl in (1, 2) and best.ngroup >= 0
+        assert best.tile_cells in (24, 32, 40, 48) and best.vpl in (1, 2) and best.ngroup >= 0
         case = mg.Case(path)
         rho, u, T, mask = case.initial_fields()
         s = mg.Solver(case=case, precision=mg.FP32, mask=mask)  # shape 0: the remembered one
