@@ -256,6 +256,57 @@ def run_reference(args, rank: int, dist: Dist) -> None:
         print(json.dumps(line), flush=True)
 
 
+def run_other_configs(tmp: str) -> dict:
+    """Config 1 (incompressible BGK cavity, 64^2 quads, D2Q9, FP64, the full 2000 steps) against the
+    oracle run alongside, and config 3 (61^2 quads, hGH 28^2, Kn 0.075) in FP32 against FP64."""
+    import cases
+    import meso_gpu as mg
+    import meso_oracle as mo
+
+    out = {}
+    p1 = cases.config1(os.path.join(tmp, "c1"), 2000)
+    c1 = mg.Case(p1)
+    rho, u, T, mask = c1.initial_fields()
+    s = mg.Solver(case=c1, precision=mg.FP64, mask=mask)
+    s.init_macros(rho, u, T, None, 0)
+    s.step(2000)
+    ms = s.last_step_ms()
+    a = s.macros(c1.ncell)
+    s.close()
+    o = mo.Oracle(c1, min(os.cpu_count() or 1, c1.nv), mask)
+    o.init(rho, u, T, None, 0)
+    t0 = time.perf_counter()
+    o.step(2000)
+    cpu_s = time.perf_counter() - t0
+    b = o.macros()
+    o.close()
+    cx1 = c1.ncell * c1.nv * 2000
+    out["config1_bgk_fp64"] = {"cells": c1.ncell, "velocities": c1.nv, "steps": 2000,
+                               "value": cx1 / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / 2000,
+                               "cpu_port_value": cx1 / cpu_s, "cpu_cores": min(os.cpu_count() or 1, c1.nv),
+                               "max_rel_err_vs_oracle": {"rho": relerr(a[0], b[0]), "u": relerr(a[1], b[1])},
+                               "note": "4096 cells x 9 velocities fits in L2; launch- and latency-bound"}
+    p3 = cases.config3(os.path.join(tmp, "c3"), 5000, "fp32")
+    c3 = mg.Case(p3)
+    rho, u, T, mask = c3.initial_fields()
+    res = {}
+    for prec in (mg.FP32, mg.FP64):
+        s = mg.Solver(case=c3, precision=prec, mask=mask)
+        s.init_macros(rho, u, T, None, 0)
+        s.step(3)
+        s.step(200)
+        res[prec] = (s.last_step_ms() / 200, s.macros(c3.ncell))
+        s.close()
+    cx3 = c3.ncell * c3.nv
+    out["config3_shakhov_fp32"] = {"cells": c3.ncell, "velocities": c3.nv, "steps": 203,
+                                   "value": cx3 / (res[mg.FP32][0] * 1e-3), "unit": UNIT,
+                                   "ms_per_step": res[mg.FP32][0], "fp64_ms_per_step": res[mg.FP64][0],
+                                   "fp32_error_vs_fp64": {k: relerr(x, y) for k, x, y in
+                                                          zip(("rho", "u", "T", "q"), res[mg.FP32][1], res[mg.FP64][1])},
+                                   "note": "state 23 MB fits in L2"}
+    return out
+
+
 def run_batched(tmp: str, steps: int = 20, warm: int = 3, autotune: bool = True) -> dict:
     """Config 4: 64 cavity instances (seeded draws of mesh side, Kn, velocity set, lid) in one batch."""
     import cases
@@ -503,6 +554,7 @@ def main() -> int:
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(path, 12.0, os.cpu_count() or 1)
         if not args.no_batched:
+            line["other_configs"] = run_other_configs(tmp)
             line["batched"] = run_batched(tmp)
         if not args.no_served:
             line["served"] = run_served(tmp, count=args.served_count)

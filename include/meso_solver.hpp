@@ -1,0 +1,149 @@
+// meso_solver.hpp -- C++ drop-in for the meso-lts solver classes, over the C-ABI of meso_gpu.h.
+//
+// The reference runs each solve through handle_solver<SolverClass> (src/meso/exec.cpp:141-165):
+//
+//     SolverClass solver(parser, config);
+//     solver.initial();
+//     solver.output();
+//     for (int i = 0; (i < solver.max_step()) || (solver.max_step() < 0); ++i) {
+//         solver.do_step();
+//         if (not solver.get_run_state()) break;
+//         if (solver.step % solver.write_interval() == 0) solver.output();
+//     }
+//     solver.output();
+//
+// MESO::GPU::Solver has the members that loop and output() use, with the reference's names and
+// meaning (include/solver/boltzmann/cdugks_shakhov.h:4-60, include/solver/solver.h:22-46): step,
+// solution_time, rho_cell, vel_cell, T_cell, q_cell, initial(), do_step(), output(),
+// get_run_state(), max_step(), write_interval().  One class serves the three solver kinds; the case
+// file's "solver" key picks the kind, as main.cpp:49-54 does.  Errors surface as the reference's
+// exceptions: std::invalid_argument for bad input, std::runtime_error otherwise.  The macroscopic
+// Fields are copied from the device when read through sync() (do_step() syncs at the residual
+// interval and when the run state turns false, output() and the destructor need no sync).
+#ifndef MESO_SOLVER_HPP
+#define MESO_SOLVER_HPP
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "meso_gpu.h"
+
+namespace MESO {
+namespace GPU {
+
+// Vector and Field<T>: the parts of include/core/vector.h and include/mesh/object.h:42-75 the step
+// loop and output read.
+struct Vector {
+    double x = 0.0, y = 0.0, z = 0.0;
+};
+
+template <class T> struct Field {
+    int len = 0;
+    std::vector<T> values;
+    T &operator[](int i) { return values[(size_t)i]; }
+    const T &operator[](int i) const { return values[(size_t)i]; }
+};
+
+class Solver {
+public:
+    int step = 0;
+    double solution_time = 0.0;
+    Field<double> rho_cell, T_cell;
+    Field<Vector> vel_cell, q_cell;
+
+    // precision: MESO_FP64 (the parity form), MESO_FP32, or -1 for the case file's "gpu-precision"
+    explicit Solver(const std::string &case_file, int precision = -1) {
+        meso_case *k = nullptr;
+        check(meso_case_load(case_file.c_str(), &k));
+        meso_mesh_desc m;
+        int32_t rnp = 0, ol = 0, onp = 0;
+        int rc = meso_case_mesh(k, &m);
+        if (rc == MESO_OK) rc = meso_case_loop_settings(k, &max_step_, &write_interval_, &rnp, &ol, &onp);
+        meso_case_free(k);
+        check(rc);
+        ncell_ = m.ncell;
+        check(meso_ctx_create_from_case(case_file.c_str(), precision, &ctx_));
+        resize();
+    }
+    ~Solver() { meso_ctx_destroy(ctx_); }
+    Solver(const Solver &) = delete;
+    Solver &operator=(const Solver &) = delete;
+
+    void initial() {
+        check(meso_initial(ctx_));
+        refresh_status();
+        sync();
+    }
+
+    void do_step() {
+        int32_t done = 0;
+        const int rc = meso_step(ctx_, 1, &done);
+        if (rc != MESO_OK && rc != MESO_ERR_NAN) check(rc);  // NaN: run_state turns false, as in the reference
+        refresh_status();
+        meso_params p;
+        check(meso_get_params(ctx_, &p));
+        if (!run_state_ || (p.residual_interval > 0 && step % p.residual_interval == 0)) sync();
+    }
+
+    void output() { check(meso_output(ctx_)); }
+    bool get_run_state() const { return run_state_; }
+    int max_step() const { return max_step_; }
+    int write_interval() const { return write_interval_; }
+
+    // Copies the macroscopic fields from the device (original cell order).
+    void sync() {
+        std::vector<double> u(3 * (size_t)ncell_), q(3 * (size_t)ncell_);
+        check(meso_get_macros(ctx_, rho_cell.values.data(), u.data(), T_cell.values.data(), q.data()));
+        for (int i = 0; i < ncell_; ++i) {
+            vel_cell.values[(size_t)i] = {u[3 * (size_t)i], u[3 * (size_t)i + 1], u[3 * (size_t)i + 2]};
+            q_cell.values[(size_t)i] = {q[3 * (size_t)i], q[3 * (size_t)i + 1], q[3 * (size_t)i + 2]};
+        }
+    }
+
+    meso_ctx *handle() { return ctx_; }
+
+private:
+    static void check(int rc) {
+        if (rc == MESO_OK) return;
+        if (rc == MESO_ERR_INVALID || rc == MESO_ERR_IO) throw std::invalid_argument(meso_last_error());
+        throw std::runtime_error(meso_last_error());
+    }
+    void resize() {
+        rho_cell.len = T_cell.len = vel_cell.len = q_cell.len = ncell_;
+        rho_cell.values.assign((size_t)ncell_, 0.0);
+        T_cell.values.assign((size_t)ncell_, 0.0);
+        vel_cell.values.assign((size_t)ncell_, Vector());
+        q_cell.values.assign((size_t)ncell_, Vector());
+    }
+    void refresh_status() {
+        meso_status st;
+        check(meso_get_status(ctx_, &st));
+        step = st.step;
+        solution_time = st.solution_time;
+        run_state_ = st.run_state != 0;
+    }
+
+    meso_ctx *ctx_ = nullptr;
+    int ncell_ = 0;
+    int32_t max_step_ = 0, write_interval_ = 1;
+    bool run_state_ = true;
+};
+
+// The reference's per-solve loop (src/meso/exec.cpp:141-165) over the GPU solver.
+inline int handle_solver(Solver &solver) {
+    solver.initial();
+    solver.output();
+    for (int i = 0; (i < solver.max_step()) || (solver.max_step() < 0); ++i) {
+        solver.do_step();
+        if (!solver.get_run_state()) break;
+        if (solver.write_interval() > 0 && solver.step % solver.write_interval() == 0) solver.output();
+    }
+    solver.output();
+    return 0;
+}
+
+}  // namespace GPU
+}  // namespace MESO
+
+#endif  // MESO_SOLVER_HPP

@@ -1,0 +1,54 @@
+// meso_gpu_run: the reference's per-solve loop (src/meso/exec.cpp:141-165) over the GPU solver.
+//
+//   meso_gpu_run <case-file> [fp64|fp32] [--dump <file>]
+//
+// Runs initial(), output(), do_step() until max-step or run_state false (output() every
+// write-interval), output(), as the reference's meso-mpi does for one case file, with the
+// MESO::GPU::Solver drop-in (include/meso_solver.hpp).  --dump writes the final macroscopic fields
+// as raw doubles: ncell, step, solution_time, rho[ncell], u[3 ncell], T[ncell], q[3 ncell].
+#include <cstdio>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <vector>
+
+#include "meso_solver.hpp"
+
+int main(int argc, char **argv) {
+    if (argc < 2) {
+        std::fprintf(stderr, "usage: %s <case-file> [fp64|fp32] [--dump <file>]\n", argv[0]);
+        return 2;
+    }
+    int precision = -1;
+    std::string dump;
+    for (int i = 2; i < argc; ++i) {
+        if (!std::strcmp(argv[i], "fp64")) precision = MESO_FP64;
+        else if (!std::strcmp(argv[i], "fp32")) precision = MESO_FP32;
+        else if (!std::strcmp(argv[i], "--dump") && i + 1 < argc) dump = argv[++i];
+    }
+    try {
+        MESO::GPU::Solver solver(argv[1], precision);
+        MESO::GPU::handle_solver(solver);
+        solver.sync();
+        std::printf("step %d  solution_time %.17g  run_state %d\n", solver.step, solver.solution_time,
+                    solver.get_run_state() ? 1 : 0);
+        if (!dump.empty()) {
+            FILE *f = std::fopen(dump.c_str(), "wb");
+            if (!f) throw std::runtime_error("cannot write " + dump);
+            const double head[3] = {(double)solver.rho_cell.len, (double)solver.step, solver.solution_time};
+            std::fwrite(head, sizeof(double), 3, f);
+            std::fwrite(solver.rho_cell.values.data(), sizeof(double), solver.rho_cell.values.size(), f);
+            for (const auto &v : solver.vel_cell.values) std::fwrite(&v, sizeof(double), 3, f);
+            std::fwrite(solver.T_cell.values.data(), sizeof(double), solver.T_cell.values.size(), f);
+            for (const auto &v : solver.q_cell.values) std::fwrite(&v, sizeof(double), 3, f);
+            std::fclose(f);
+        }
+    } catch (const std::invalid_argument &e) {
+        std::fprintf(stderr, "invalid argument: %s\n", e.what());
+        return 1;
+    } catch (const std::exception &e) {
+        std::fprintf(stderr, "error: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}

@@ -90,6 +90,20 @@ def build_library(force: bool = False, jobs: int | None = None) -> str:
     return LIB
 
 
+APP = os.path.join(LIBDIR, "meso_gpu_run")
+
+
+def build_apps(force: bool = False) -> str:
+    """The C++ drop-in driver (apps/meso_gpu_run.cpp over include/meso_solver.hpp)."""
+    src = os.path.join(PKG, "apps", "meso_gpu_run.cpp")
+    hdr_t = max(os.path.getmtime(os.path.join(INCLUDE, "meso_solver.hpp")),
+                os.path.getmtime(os.path.join(INCLUDE, "meso_gpu.h")), os.path.getmtime(LIB))
+    if force or _stale(src, APP, hdr_t):
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-I" + INCLUDE, src, "-o", APP, "-L" + LIBDIR, "-lmeso_gpu",
+              "-Wl,-rpath," + LIBDIR])
+    return APP
+
+
 def build_oracle(force: bool = False) -> str:
     src = os.path.join(ORACLE, "meso_oracle.c")
     os.makedirs(os.path.dirname(ORACLE_LIB), exist_ok=True)
@@ -115,6 +129,7 @@ def build_all(force: bool = False) -> None:
         b = ex.submit(build_oracle, force)
         a.result()
         b.result()
+    build_apps(force)
     build_reference()
 
 

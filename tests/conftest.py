@@ -24,6 +24,7 @@ def _built():
 
     build.build_library()
     build.build_oracle()
+    build.build_apps()
     yield
 
 
