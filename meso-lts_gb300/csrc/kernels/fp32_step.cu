@@ -64,6 +64,14 @@ __device__ __forceinline__ float fast_ex2(float x) {
     return y;
 }
 
+// The same with the face's FP64 normal and the velocity's FP64 components already at hand.
+__device__ __forceinline__ int classify_r(double2 n, double x64, double y64, float d32, float margin) {
+    if (d32 > margin) return 0;
+    if (d32 < -margin) return 1;
+    const double d = __dadd_rn(__dmul_rn(n.x, x64), __dmul_rn(n.y, y64));
+    return d >= kVSMALL ? 0 : (d < -kVSMALL ? 1 : 2);
+}
+
 // 0: from the owner (n0.xi >= VSMALL), 1: from the neighbour (< -VSMALL), 2: between.
 __device__ __forceinline__ int classify(const F32Inst &I, int f, int p, float d32, float xx, float xy) {
     const float margin = 1e-5f * (fabsf(xx) + fabsf(xy));
@@ -209,6 +217,7 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
 }
 
 struct OwnedFace {     // P1: one face owned by the tile
+    double2 n64;       // FP64 normal for the exact upwind test
     float2 n, fdo, fdn;
     int bnd, face;
     unsigned short os, ns;
@@ -389,6 +398,7 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
         for (int f = threadIdx.x; f < nOF; f += kT) {
             const int g = fs + f;
             OwnedFace o;
+            o.n64 = I.fn64[g];
             o.n = I.fn32[g];
             o.fdo = I.fdo[g];
             o.fdn = I.fdn[g];
@@ -406,7 +416,8 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
             next_chunk<VPL>(S, NVp, ch, ch1, buf, sm);
             gradients(sm, buf, grad_on);
             __syncthreads();
-            float xx[VPL], xy[VPL], hx[VPL], hy[VPL];
+            float xx[VPL], xy[VPL], hx[VPL], hy[VPL], mg[VPL];
+            double x64[VPL], y64[VPL];
             int p[VPL];
 #pragma unroll
             for (int v = 0; v < VPL; ++v) {
@@ -414,16 +425,25 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
                 const float4 t = vt32[p[v]];
                 xx[v] = t.x;
                 xy[v] = t.y;
+                x64[v] = I.xi64x[p[v]];
+                y64[v] = I.xi64y[p[v]];
+                mg[v] = 1e-5f * (fabsf(xx[v]) + fabsf(xy[v]));
                 hx[v] = hdt * xx[v];
                 hy[v] = hdt * xy[v];
             }
             for (int fl = warp; fl < nOF; fl += F32_WARPS) {
                 const OwnedFace o = sm.u.p1.of[fl];
-                float2 *dst = o.bnd >= 0 ? bnd_in + (size_t)o.bnd * NVp : fbar + (size_t)o.face * NVp;
+                if (o.bnd >= 0) {  // own = neighbour: every upwind choice gives the owner's reconstruction
+                    float2 *dst = bnd_in + (size_t)o.bnd * NVp;
 #pragma unroll
-                for (int v = 0; v < VPL; ++v) {
-                    const int cls = classify(I, o.face, p[v], fmaf(o.n.x, xx[v], o.n.y * xy[v]), xx[v], xy[v]);
-                    dst[p[v]] = face_bar(sm, buf, v, cls, o.os, o.ns, o.fdo, o.fdn, hx[v], hy[v]);
+                    for (int v = 0; v < VPL; ++v) dst[p[v]] = recon(sm, buf, o.os, v, o.fdo, hx[v], hy[v]);
+                } else {
+                    float2 *dst = fbar + (size_t)o.face * NVp;
+#pragma unroll
+                    for (int v = 0; v < VPL; ++v) {
+                        const int cls = classify_r(o.n64, x64[v], y64[v], fmaf(o.n.x, xx[v], o.n.y * xy[v]), mg[v]);
+                        dst[p[v]] = face_bar(sm, buf, v, cls, o.os, o.ns, o.fdo, o.fdn, hx[v], hy[v]);
+                    }
                 }
             }
             __syncthreads();
