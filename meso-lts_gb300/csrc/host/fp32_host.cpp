@@ -148,8 +148,6 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.face_nei_slot = up(A, P.face_nei_slot, s);
         I.tile_tf_ptr = up(A, P.tile_tf_ptr, s);
         I.tf_face = up(A, P.tf_face, s);
-        I.tf_os = up(A, P.tf_os, s);
-        I.tf_ns = up(A, P.tf_ns, s);
         I.cf_tf = up(A, P.cf_tf, s);
         I.cf_ptr = c->dm.cf_ptr;
         I.cf_face = c->dm.cf_face;

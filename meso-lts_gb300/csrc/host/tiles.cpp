@@ -217,8 +217,8 @@ bool build_tile_plan(const meso_mesh_desc &m, const Renumbering &rn, const std::
             P.face_nei_slot[fcur] = (uint16_t)slot_of[fnei[fcur]];
             ++fcur;
         }
-        // per cell-face: slot of the cell on the other side, and the tile-face list
-        const size_t cf0 = P.cf_oslot.size();
+        // per cell-face entry: its face in the tile-face list
+        const size_t cf0 = P.cf_tf.size();
         const int tf0 = (int)P.tf_face.size();
         P.tile_tf_ptr.push_back(tf0);
         bool tf_ok = true;
@@ -226,20 +226,16 @@ bool build_tile_plan(const meso_mesh_desc &m, const Renumbering &rn, const std::
             int o = rn.cell_new2old[c];
             for (int j = m.cell_face_ptr[o]; j < m.cell_face_ptr[o + 1]; ++j) {
                 int f = rn.face_old2new[m.cell_face[j]];
-                int other = fown[f] == c ? fnei[f] : fown[f];
-                P.cf_oslot.push_back((uint16_t)slot_of[other]);
                 if (fstamp[f] != t) {
                     fstamp[f] = t;
                     flocal[f] = (int)P.tf_face.size() - tf0;
                     P.tf_face.push_back(f);
-                    P.tf_os.push_back((uint16_t)slot_of[fown[f]]);
-                    P.tf_ns.push_back((uint16_t)slot_of[fnei[f]]);
                 }
                 tf_ok = tf_ok && flocal[f] < 0x80;
                 P.cf_tf.push_back((uint8_t)((flocal[f] & 0x7f) | (fown[f] == c ? 0 : 0x80)));
             }
         }
-        P.max_cf = std::max(P.max_cf, (int)(P.cf_oslot.size() - cf0));
+        P.max_cf = std::max(P.max_cf, (int)(P.cf_tf.size() - cf0));
         P.max_tf = std::max(P.max_tf, tf_ok ? (int)P.tf_face.size() - tf0 : 1 << 20);
         P.max_cells = std::max(P.max_cells, n);
         P.max_slots = std::max(P.max_slots, (int)slots.size());

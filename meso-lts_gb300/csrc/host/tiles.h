@@ -28,11 +28,9 @@ struct TilePlan {
     std::vector<float> gs_ax, gs_ay;                 // w_j (Cx . dr_j), w_j (Cy . dr_j)
     std::vector<int> tile_fstart;                    // [ntile+1] owned face range
     std::vector<uint16_t> face_own_slot, face_nei_slot;  // per face, in its owner tile
-    std::vector<uint16_t> cf_oslot;                  // per cell-face entry: slot of the other cell in the cell's tile
     // faces that touch a tile cell, each once per tile (the update kernel evaluates each once)
     std::vector<int> tile_tf_ptr;                    // [ntile+1]
     std::vector<int> tf_face;                        // renumbered face id
-    std::vector<uint16_t> tf_os, tf_ns;              // slots of the face's owner and neighbour
     std::vector<uint8_t> cf_tf;                      // per cell-face entry: tile-face index, | 0x80 when the cell
                                                      // is the face's neighbour (flux counted negative)
 };

@@ -71,7 +71,6 @@ struct F32Inst {
     const int *tile_fstart;
     const uint16_t *face_own_slot, *face_nei_slot;
     const int *tile_tf_ptr, *tf_face;
-    const uint16_t *tf_os, *tf_ns;
     const uint8_t *cf_tf;
     // mesh (renumbered)
     const int *cf_ptr, *cf_face, *fown, *fnei, *fbnd, *bface, *fmark;
