@@ -33,6 +33,7 @@ struct meso_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    meso::StepFork fork;  // side stream and events of the captured step's branch
     int launches_per_step = 0;
     double last_ms = 0.0;
     int64_t last_launches = 0;
@@ -66,9 +67,15 @@ int rebuild(meso_batch *b) {
         return fail(MESO_ERR_OOM, "batch work-list allocation failed");
     if (!b->use_graph) return MESO_OK;
     int64_t n = 0;
-    cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    cudaError_t e = cudaSuccess;
+    if (!b->fork.side) {
+        e = cudaStreamCreateWithFlags(&b->fork.side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork.fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork.join, cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        const int rc = meso::fp32_step(b->fs, b->stream, &n);
+        const int rc = meso::fp32_step(b->fs, b->stream, &n, nullptr, &b->fork);
         e = cudaStreamEndCapture(b->stream, &b->graph);
         if (rc == 0 && e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
     }
@@ -153,6 +160,9 @@ void meso_batch_destroy(meso_batch *b) {
         if (c && c->batch == b) c->batch = nullptr;
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->fork.side) cudaStreamDestroy(b->fork.side);
+    if (b->fork.fork) cudaEventDestroy(b->fork.fork);
+    if (b->fork.join) cudaEventDestroy(b->fork.join);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }

@@ -464,8 +464,15 @@ bool capture_f32_graph(meso_ctx *c) {
     c->f32_graph = nullptr;
     cudaGraph_t g = nullptr;
     int64_t n = 0;
+    if (!c->f32_fork.side &&
+        (cudaStreamCreateWithFlags(&c->f32_fork.side, cudaStreamNonBlocking) != cudaSuccess ||
+         cudaEventCreateWithFlags(&c->f32_fork.fork, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&c->f32_fork.join, cudaEventDisableTiming) != cudaSuccess)) {
+        cudaGetLastError();
+        return false;
+    }
     if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
-    const int rc = meso::fp32_step(c->fs, c->stream, &n);
+    const int rc = meso::fp32_step(c->fs, c->stream, &n, nullptr, &c->f32_fork);
     const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     bool ok = rc == 0 && e == cudaSuccess && cudaGraphInstantiate(&c->f32_graph, g, 0) == cudaSuccess;
     if (g) cudaGraphDestroy(g);
@@ -805,6 +812,9 @@ void meso_ctx_destroy(meso_ctx *c) {
     if (c->batch) meso_host::batch_forget(c->batch, c);
     if (c->f32_graph) cudaGraphExecDestroy(c->f32_graph);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->f32_fork.side) cudaStreamDestroy(c->f32_fork.side);
+    if (c->f32_fork.fork) cudaEventDestroy(c->f32_fork.fork);
+    if (c->f32_fork.join) cudaEventDestroy(c->f32_fork.join);
     free_fp32_launch(c->fs, c->fs_owned);
     c->arena.release();
     if (c->h_status) cudaFreeHost(c->h_status);

@@ -87,6 +87,7 @@ struct meso_ctx {
     std::time_t case_mtime = 0;
     int f32_version = 0;  // bumped when the FP32 instance's settings change on the device
     cudaGraphExec_t f32_graph = nullptr;  // the FP32 step's launches, captured once
+    meso::StepFork f32_fork;              // side stream and events of the captured step's branch
     int f32_graph_version = -1;
     int64_t f32_graph_launches = 0;
     meso_batch *batch = nullptr;  // the batch this context is a member of, if any

@@ -1248,7 +1248,7 @@ int fp32_configure(int device) {
 const char *const kFp32Phases[] = {"k32_reconstruct", "k32_face_moments+macros", "k32_face_eqflux", "k32_boundary",
                                    "k32_cell_macros", "k32_update", "k32_heat_flux+repair+end"};
 
-int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev) {
+int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev, const StepFork *fork) {
     const int sms = s.num_sms;
     const int cap = sms * 32;
     // one persistent CTA per SM; items of vpl == 2 instances, then those of vpl == 1, each its own launch
@@ -1278,11 +1278,22 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     k32_face_macros<<<grid_of(s.total_faces, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
                                                                           s.total_faces);
     mark(2);
+    const bool branch = fork && !ev && s.total_bnd > 0;
+    if (branch) {  // boundary faces on the side stream, interior faces' equilibrium fluxes here
+        cudaEventRecord(fork->fork, stream);
+        cudaStreamWaitEvent(fork->side, fork->fork, 0);
+        k32_boundary<<<grid_of(s.total_bnd, 1, cap), 256, 0, fork->side>>>(s.d_inst, s.d_bnd_items, s.ninst,
+                                                                           s.total_bnd);
+        cudaEventRecord(fork->join, fork->side);
+    }
     k32_face_eqflux<<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
                                                                         s.total_faces);
     mark(3);
     n += 3;
-    if (s.total_bnd > 0) {
+    if (branch) {
+        cudaStreamWaitEvent(stream, fork->join, 0);
+        ++n;
+    } else if (s.total_bnd > 0) {
         k32_boundary<<<grid_of(s.total_bnd, 1, cap), 256, 0, stream>>>(s.d_inst, s.d_bnd_items, s.ninst, s.total_bnd);
         ++n;
     }

@@ -126,8 +126,18 @@ struct Fp32State {
 int fp32_configure(int device);
 constexpr int F32_NPHASE = 7;
 extern const char *const kFp32Phases[F32_NPHASE];
-// One step of every instance; ev (may be null) receives F32_NPHASE + 1 events around the phases.
-int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev = nullptr);
+// A second stream and two events with which the boundary kernel runs beside the face-equilibrium
+// kernel (they depend on the same face macros and write disjoint faces).  Used when the step is
+// captured as a graph, where the fork and join become graph edges.
+struct StepFork {
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+// One step of every instance; ev (may be null) receives F32_NPHASE + 1 events around the phases
+// (the phases then run in order on `stream`); fork (may be null) runs the boundary kernel beside
+// the face-equilibrium kernel.
+int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev = nullptr,
+              const StepFork *fork = nullptr);
 // Once per instance set-up, after the instances are on the device.
 int fp32_prepare(const Fp32State &s, cudaStream_t stream);
 int fp32_init(const Fp32State &s, int mode, cudaStream_t stream);
