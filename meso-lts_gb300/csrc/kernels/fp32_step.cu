@@ -253,7 +253,6 @@ template <int VPL> struct __align__(128) UpdSmem {
     const float2 *src[F32_MAX_TF];              // where each tile face's flux values are, [NVp]
     CellK ck[F32_MAX_CELLS];
     int cf_off[F32_MAX_CELLS + 1];
-    float acc[F32_MAX_CELLS * 4];
     unsigned char cft[F32_MAX_CF];              // per cell-face entry: tile face | 0x80 if the cell is its neighbour
     int nc, ntf, cs;
 };
@@ -502,13 +501,17 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
             const int f = I.tf_face[q0 + q], b = I.fbnd[f];
             sm.src[q] = b >= 0 ? I.bnd_out + (size_t)b * NVp : I.fbar + (size_t)f * NVp;
         }
-        for (int k = threadIdx.x; k < nc * 4; k += kT) sm.acc[k] = 0.f;
         if (threadIdx.x == 0) {
             sm.nc = nc;
             sm.ntf = ntf;
             sm.cs = cs;
         }
         __syncthreads();
+        // heat-flux partials of this warp's cells (cl = warp + 16 r): per lane, compensated, across chunks
+        constexpr int RC = (F32_MAX_CELLS + F32_WARPS - 1) / F32_WARPS;
+        float qs[RC][2], qc[RC][2];
+#pragma unroll
+        for (int r = 0; r < RC; ++r) qs[r][0] = qs[r][1] = qc[r][0] = qc[r][1] = 0.f;
         load_upd_chunk<VPL>(S, NVp, ch0, 0, sm);
         for (int ch = ch0; ch < ch1; ++ch) {
             const int buf = (ch - ch0) & 1;
@@ -531,7 +534,10 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                 w[v] = t.z;
                 g0[v] = t.w;
             }
-            for (int cl = warp; cl < nc; cl += F32_WARPS) {
+#pragma unroll
+            for (int r = 0; r < RC; ++r) {
+                const int cl = warp + F32_WARPS * r;
+                if (cl >= nc) break;
                 float fg[VPL], fh[VPL];
 #pragma unroll
                 for (int v = 0; v < VPL; ++v) fg[v] = fh[v] = 0.f;
@@ -568,18 +574,25 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                     qv[0] = fmaf(hw, cx, qv[0]);
                     qv[1] = fmaf(hw, cy, qv[1]);
                 }
-                warp_sum(qv);
-                if (lane < 2) {
-                    float *a = sm.acc + cl * 4 + 2 * lane;
-                    kahan(a[0], a[1], lane == 0 ? qv[0] : qv[1]);
-                }
+                kahan(qs[r][0], qc[r][0], qv[0]);
+                kahan(qs[r][1], qc[r][1], qv[1]);
             }
             __syncthreads();
         }
-        for (int k = threadIdx.x; k < nc * 2; k += kT) {
-            const int cl = k >> 1, comp = k & 1;
-            I.qpart[((size_t)grp * I.C + cs + cl) * 2 + comp] =
-                (double)sm.acc[cl * 4 + 2 * comp] - (double)sm.acc[cl * 4 + 2 * comp + 1];
+#pragma unroll
+        for (int r = 0; r < RC; ++r) {  // one warp reduction per cell and item, in FP64
+            const int cl = warp + F32_WARPS * r;
+            if (cl >= nc) break;
+            double q0 = (double)qs[r][0] - (double)qc[r][0], q1 = (double)qs[r][1] - (double)qc[r][1];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                q0 += __shfl_xor_sync(0xffffffffu, q0, o);
+                q1 += __shfl_xor_sync(0xffffffffu, q1, o);
+            }
+            if (lane == 0) {
+                I.qpart[((size_t)grp * I.C + cs + cl) * 2] = q0;
+                I.qpart[((size_t)grp * I.C + cs + cl) * 2 + 1] = q1;
+            }
         }
         __syncthreads();
     }
