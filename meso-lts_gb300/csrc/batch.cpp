@@ -9,8 +9,9 @@
 //
 // Each member keeps the reference's per-solve bookkeeping (step, solution
 // time, residual every residual_interval of its own steps, the 10-check
-// convergence counter, cdugks_shakhov.cpp:724-764).  A member that converges is
-// halted on the device at once and leaves the work list at the next call.
+// convergence counter, cdugks_shakhov.cpp:724-764).  The check runs on the
+// device after each step (k32_residual); a member that converges is halted
+// there at once and leaves the work list at the next call.
 #include <algorithm>
 #include <climits>
 #include <cstring>
@@ -100,13 +101,6 @@ int launch(meso_batch *b) {
     return MESO_OK;
 }
 
-int set_halt(meso_batch *b, meso_ctx *c) {
-    const int one = 1;
-    if (cudaMemcpyAsync(&c->d_status->halt, &one, sizeof(int), cudaMemcpyHostToDevice, b->stream) != cudaSuccess)
-        return fail(MESO_ERR_CUDA, "cannot halt a converged member");
-    return MESO_OK;
-}
-
 }  // namespace
 
 extern "C" {
@@ -181,43 +175,17 @@ int meso_batch_step(meso_batch *b, int32_t nsteps, int32_t *nrunning) {
     }
     int rc = MESO_OK;
     if (stale && (rc = rebuild(b))) return rc;
-    std::vector<int> start(n), issued(n, 0);
+    std::vector<int> start(n);
     for (int i = 0; i < n; ++i) start[i] = b->members[i] ? b->members[i]->step : 0;
     b->last_launches = 0;
     cudaEventRecord(b->ev0, b->stream);
     int nact = 0;
     for (int i = 0; i < n; ++i) nact += b->active[i] && running(b->members[i]);
-    for (int it = 0; it < nsteps && nact > 0; ++it) {
+    // The residual check and the convergence counter run on the device (k32_residual), so the
+    // steps go out back to back; a member that converges or fails is halted there and its kernels
+    // skip it from the next step on.
+    for (int it = 0; it < nsteps && nact > 0; ++it)
         if ((rc = launch(b))) return rc;
-        bool check = false;
-        for (int i = 0; i < n; ++i) {
-            meso_ctx *c = b->members[i];
-            if (!b->active[i] || !running(c)) continue;
-            ++issued[i];
-            const int ri = c->params.residual_interval;
-            check = check || (ri > 0 && (start[i] + issued[i]) % ri == 0);
-        }
-        if (!check) continue;
-        if (cudaStreamSynchronize(b->stream) != cudaSuccess)
-            return fail(MESO_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString(cudaGetLastError()));
-        for (int i = 0; i < n; ++i) {
-            meso_ctx *c = b->members[i];
-            if (!b->active[i] || !running(c)) continue;
-            const int ri = c->params.residual_interval;
-            if (!(ri > 0 && (start[i] + issued[i]) % ri == 0)) continue;
-            if ((rc = meso_host::ctx_read_status(c))) return rc;
-            if (c->h_status->stop_step != INT_MAX || c->h_status->timeout) {
-                c->run_state = 0;  // unmasked NaN / T < 0: the member's kernels already skip it
-                --nact;
-                continue;
-            }
-            if ((rc = meso_host::ctx_residual_check(c))) return rc;
-            if (!running(c)) {  // converged
-                if ((rc = set_halt(b, c))) return rc;
-                --nact;
-            }
-        }
-    }
     cudaEventRecord(b->ev1, b->stream);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess)
         return fail(MESO_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString(cudaGetLastError()));
@@ -232,6 +200,7 @@ int meso_batch_step(meso_batch *b, int32_t nsteps, int32_t *nrunning) {
         const int done = c->h_status->step - start[i];
         for (int k = 0; k < done; ++k) c->solution_time += c->params.dt;  // as do_step accumulates it
         c->step = c->h_status->step;
+        if ((rc = meso_host::ctx_read_resid(c))) return rc;
         if (c->h_status->stop_step != INT_MAX || c->h_status->timeout) c->run_state = 0;
         still += running(c) ? 1 : 0;
     }

@@ -511,6 +511,9 @@ int refresh_f32(meso_ctx *c) {
     I.mu0 = p.mu0;
     I.vhs = p.vhs_index;
     I.gradient = p.gradient_switch;
+    I.res_interval = p.residual_interval;
+    I.res_fields = p.residual_fields;
+    I.res_limit = p.residual_limit;
     CUDA_TRY(cudaMemcpyAsync(c->fs.d_inst, &I, sizeof(I), cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->f32_version++;
@@ -652,6 +655,15 @@ int init_common(meso_ctx *c, const double *rho, const double *u, const double *T
     c->converged = 0;
     c->converge_state = 0;
     c->initialized = true;
+    if (c->params.precision == MESO_FP32) {  // the device residual check starts from these macros
+        const meso::F32Inst &I = c->f32;
+        const size_t C = (size_t)c->C;
+        CUDA_TRY(cudaMemcpyAsync(I.rho_old, I.rho, sizeof(double) * C, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.u_old, I.u, sizeof(double) * 3 * C, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.T_old, I.T, sizeof(double) * C, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.q_old, I.q, sizeof(double) * 3 * C, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(cudaMemsetAsync(I.resid, 0, sizeof(meso::F32Resid), c->stream));
+    }
     std::vector<double> T2, q2;
     int rc = download_macros(c, c->rho_res, c->u_res, T2, q2);
     if (rc) return rc;
@@ -692,6 +704,21 @@ std::vector<double> read_vector_file(const std::string &f, int n) {
 
 namespace meso_host {
 int ctx_read_status(meso_ctx *c) { return read_status(c); }
+int ctx_read_resid(meso_ctx *c) {
+    meso::F32Resid r;
+    CUDA_TRY(cudaMemcpyAsync(&r, c->f32.resid, sizeof(r), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->converge_state = r.converge_state;
+    if (r.nres > 0) {
+        c->nres = r.nres;
+        for (int i = 0; i < r.nres && i < 8; ++i) c->last_res[i] = r.res[i];
+    }
+    if (r.converged) {
+        c->run_state = 0;
+        c->converged = 1;
+    }
+    return MESO_OK;
+}
 int ctx_residual_check(meso_ctx *c) { return residual_check(c); }
 }  // namespace meso_host
 
@@ -881,7 +908,7 @@ int meso_step(meso_ctx *c, int32_t nsteps, int32_t *steps_done) {
         ++issued;
         const int s = start + issued;
         const int ri = c->params.residual_interval;
-        if (ri > 0 && s % ri == 0) {
+        if (ri > 0 && s % ri == 0 && c->params.precision != MESO_FP32) {  // FP32: on the device
             rc = read_status(c);
             if (rc) return rc;
             if (c->h_status->stop_step != INT_MAX) {
@@ -901,6 +928,7 @@ int meso_step(meso_ctx *c, int32_t nsteps, int32_t *steps_done) {
     const int done = c->h_status->step - start;
     for (int i = 0; i < done && i < (int)dts.size(); ++i) c->solution_time += dts[i];
     c->step = c->h_status->step;
+    if (c->params.precision == MESO_FP32 && (rc = meso_host::ctx_read_resid(c))) return rc;
     if (steps_done) *steps_done = done;
     if (stopped || c->h_status->stop_step != INT_MAX) {
         c->run_state = 0;
@@ -1093,6 +1121,21 @@ int meso_restore(meso_ctx *c, const void *host, size_t bytes) {
     c->converge_state = h.converge_state;
     c->solution_time = h.solution_time;
     c->initialized = true;
+    if (c->params.precision == MESO_FP32) {  // the device residual check resumes from the snapshot
+        const meso::F32Inst &I = c->f32;
+        const size_t C = (size_t)c->C;
+        meso::F32Resid r{};
+        r.converge_state = h.converge_state;
+        r.converged = h.converged;
+        r.checks = c->params.residual_interval > 0 ? h.step / c->params.residual_interval : 0;
+        r.nres = c->nres;
+        for (int i = 0; i < 8; ++i) r.res[i] = c->last_res[i];
+        CUDA_TRY(cudaMemcpyAsync(I.resid, &r, sizeof(r), cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.rho_old, I.rho, sizeof(double) * C, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.u_old, I.u, sizeof(double) * 3 * C, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.T_old, I.T, sizeof(double) * C, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(I.q_old, I.q, sizeof(double) * 3 * C, cudaMemcpyDeviceToDevice, c->stream));
+    }
     std::vector<double> T2, q2;
     int rc = download_macros(c, c->rho_res, c->u_res, T2, q2);
     c->T_res = T2;

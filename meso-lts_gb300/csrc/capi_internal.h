@@ -43,6 +43,7 @@ void derive_kparams(const meso_params &p, int dim, meso::KParams &k);
 // Context helpers shared with the batch and server front ends (capi.cpp).
 int ctx_read_status(meso_ctx *c);    // device status -> c->h_status (syncs the context's stream)
 int ctx_residual_check(meso_ctx *c); // residual + convergence counter of do_step
+int ctx_read_resid(meso_ctx *c);     // FP32: the device residual state -> host fields
 void batch_forget(meso_batch *b, meso_ctx *c);  // batch.cpp
 bool tuned_shape(int ncell, int nface, int nv, int &tile_cells, int &vpl, int &ngroup);  // autotune.cpp
 

@@ -73,6 +73,10 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
     I.rho0 = p.rho0 > 0.0 ? p.rho0 : 1.0;
     I.hm0 = (p.K + 1.0) * p.R * p.T0;
     I.gradient = p.gradient_switch;
+    I.res_interval = p.residual_interval;
+    I.res_fields = p.residual_fields;
+    I.res_limit = p.residual_limit;
+    I.total_volume = m->total_volume;
     // renumbered face geometry and boundary index
     std::vector<int> fown(F), fnei(F), fbnd(F, -1), bface, fmark(F);
     std::vector<float2> fn32(F), fdo(F), fdn(F);
@@ -203,6 +207,12 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.fm1 = A.alloc<double>(3 * (size_t)C);
         I.fm2 = A.alloc<double>(C);
         I.repair_list = A.alloc<int>(C);
+        I.resid = A.alloc<meso::F32Resid>(1);
+        I.rho_old = A.alloc<double>(C);
+        I.u_old = A.alloc<double>(3 * (size_t)C);
+        I.T_old = A.alloc<double>(C);
+        I.q_old = A.alloc<double>(3 * (size_t)C);
+        cudaMemsetAsync(I.resid, 0, sizeof(meso::F32Resid), s);
         I.status = c->d_status;
         cudaMemsetAsync(I.S[0], 0, cv * sizeof(float2), s);
         cudaMemsetAsync(I.S[1], 0, cv * sizeof(float2), s);

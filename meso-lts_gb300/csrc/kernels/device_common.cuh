@@ -59,7 +59,7 @@ struct DStatus {
     int repair_count;   // masked cells queued for repair this step
     int repairs_total;
     int timeout;        // a bounded device wait gave up (the step's results are invalid)
-    int halt;           // set by the host: a converged member of a batch takes no more steps
+    int halt;           // set when the solve converges (k32_residual): it takes no more steps
 };
 
 __device__ __forceinline__ bool step_stopped(const DStatus *st) { return st->stop_step < st->step || st->halt; }

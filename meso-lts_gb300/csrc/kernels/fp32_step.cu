@@ -1180,6 +1180,84 @@ __global__ void k32_end_step(const F32Inst *__restrict__ insts, int ninst) {
     st->step += 1;
 }
 
+// Residual check of do_step (Solver::residual, field.cpp:223-249; counter cdugks_shakhov.cpp:747-756)
+// every res_interval completed steps, one block per instance: per field the volume-weighted mean of
+// |new - old| / |old| (MESO_RES_L2: the volume-weighted L2-relative change instead), summed per
+// thread over cells and reduced in a fixed order in FP64; then the converge counter, the halt of a
+// converged instance, and old <- new.
+__global__ void __launch_bounds__(512) k32_residual(const F32Inst *__restrict__ insts, int ninst) {
+    __shared__ double red[16][12];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = blockIdx.x; i < ninst; i += gridDim.x) {
+        const F32Inst &I = insts[i];
+        DStatus *st = I.status;
+        const int step = st->step;
+        if (I.res_interval <= 0 || step <= 0 || step % I.res_interval != 0) continue;
+        if (st->stop_step != INT_MAX || st->halt) continue;
+        F32Resid *R = I.resid;
+        if (R->checks == step / I.res_interval) continue;  // this check already ran
+        const bool l2 = (I.res_fields & MESO_RES_L2) != 0;
+        double a[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) a[k] = 0.0;
+        for (int c = threadIdx.x; c < I.C; c += blockDim.x) {
+            const double nw[6] = {I.rho[c], I.T[c], I.u[3 * c], I.u[3 * c + 1], I.q[3 * c], I.q[3 * c + 1]};
+            const double od[6] = {I.rho_old[c], I.T_old[c], I.u_old[3 * c], I.u_old[3 * c + 1], I.q_old[3 * c],
+                                  I.q_old[3 * c + 1]};
+            if (l2) {
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const double d = nw[k] - od[k];
+                    a[2 * k] += I.vol[c] * d * d;
+                    a[2 * k + 1] += I.vol[c] * od[k] * od[k];
+                }
+            } else {
+                const double wv = I.vol[c] / I.total_volume;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) a[k] += fabs((nw[k] - od[k]) / od[k]) * wv;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+            if (lane == 0) red[warp][k] = a[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t[12];
+            for (int k = 0; k < 12; ++k) {
+                t[k] = 0.0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t[k] += red[w][k];
+            }
+            const int field[6] = {MESO_RES_RHO, MESO_RES_T, MESO_RES_U, MESO_RES_U, MESO_RES_Q, MESO_RES_Q};
+            const int watch = I.res_fields & (MESO_RES_RHO | MESO_RES_T | MESO_RES_U | MESO_RES_Q);
+            bool conv = true;
+            for (int k = 0; k < 6; ++k) {
+                const double r = l2 ? (t[2 * k + 1] > 0.0 ? sqrt(t[2 * k] / t[2 * k + 1]) : sqrt(t[2 * k])) : t[k];
+                R->res[k] = r;
+                if (watch == 0 || (watch & field[k])) conv = conv && (r <= I.res_limit);
+            }
+            R->nres = 6;
+            R->checks = step / I.res_interval;
+            R->converge_state = conv ? R->converge_state + 1 : 0;
+            if (R->converge_state >= 10) {
+                R->converged = 1;
+                st->halt = 1;  // run_state false: no further steps (the reference's loop breaks here)
+            }
+        }
+        for (int c = threadIdx.x; c < I.C; c += blockDim.x) {
+            I.rho_old[c] = I.rho[c];
+            I.T_old[c] = I.T[c];
+            I.u_old[3 * c] = I.u[3 * c];
+            I.u_old[3 * c + 1] = I.u[3 * c + 1];
+            I.q_old[3 * c] = I.q[3 * c];
+            I.q_old[3 * c + 1] = I.q[3 * c + 1];
+        }
+        __syncthreads();
+    }
+}
+
 // =============================================================================
 // initial(): FP64 equilibrium per velocity, stored in FP32; FP64 moments
 // (cdugks_shakhov.cpp:81-168).  One warp per cell.
@@ -1259,7 +1337,7 @@ int fp32_configure(int device) {
 }
 
 const char *const kFp32Phases[] = {"k32_reconstruct", "k32_face_moments+macros", "k32_face_eqflux", "k32_boundary",
-                                   "k32_cell_macros", "k32_update", "k32_heat_flux+repair+end"};
+                                   "k32_cell_macros", "k32_update", "k32_heat_flux+repair+end+residual"};
 
 int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev, const StepFork *fork) {
     const int sms = s.num_sms;
@@ -1320,8 +1398,9 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
                                                                         s.total_cells, 1);
     k32_mask_repair<<<32, 256, 0, stream>>>(s.d_inst, s.ninst);
     k32_end_step<<<(s.ninst + 63) / 64, 64, 0, stream>>>(s.d_inst, s.ninst);
+    k32_residual<<<s.ninst < s.num_sms ? s.ninst : s.num_sms, 512, 0, stream>>>(s.d_inst, s.ninst);
     mark(7);
-    n += 4;
+    n += 5;
     if (launches) *launches += n;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

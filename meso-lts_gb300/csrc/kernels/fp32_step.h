@@ -42,6 +42,16 @@ struct EqP {
     float dhm;  // (K + 3 - D) R (T - T0)
 };
 
+// Residual check state of one instance (the reference's Res[...] print list and converge counter,
+// cdugks_shakhov.cpp:729-757), kept on the device.
+struct F32Resid {
+    double res[8];        // last residuals: rho, T, u (D components), q (D components)
+    int nres;
+    int converge_state;   // consecutive checks at or below the limit
+    int converged;        // 1 once converge_state reached 10 (the instance is then halted)
+    int checks;
+};
+
 // Face equilibrium and blend weights.
 struct FaceK {
     EqP e;
@@ -64,6 +74,9 @@ struct F32Inst {
     double hm0;
     double gmom[10];  // sum w g0 xi^a over the velocity set: 1, x, y, xx, xy, yy, xxx, xxy, xyy, yyy
     int gradient;
+    // residual check and convergence counter of do_step, on the device (k32_residual)
+    int res_interval, res_fields;
+    double res_limit, total_volume;
     // tile plan
     const int *tile_cstart, *tile_ncell, *tile_slot_ptr, *slot_cell, *tile_gslots, *tile_gsp_off, *gs_ptr;
     const uint16_t *gs_nbr;
@@ -106,6 +119,8 @@ struct F32Inst {
     double *fm0, *fm1, *fm2;   // flux moments
     int *repair_list;
     DStatus *status;
+    F32Resid *resid;           // residual state (device)
+    double *rho_old, *u_old, *T_old, *q_old;  // macros at the last residual check
 };
 
 // Host-side handle of one or more instances sharing the phase launches.
