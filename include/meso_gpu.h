@@ -347,6 +347,10 @@ int32_t meso_batch_size(meso_batch *batch);
 /* Device time of the last meso_batch_step call (ms) and the kernel launches it issued. */
 double meso_batch_last_step_ms(meso_batch *batch);
 int64_t meso_batch_last_step_launches(meso_batch *batch);
+/* nsteps steps of the batch with the kernels launched one by one and timed per phase (names as
+ * meso_phase_name of a member): ms[k] receives the mean device time of phase k per step.  No
+ * counterpart in the reference. */
+int meso_batch_phase_times(meso_batch *batch, int32_t nsteps, double *ms, int32_t max_phases, int32_t *nphases);
 
 /* ---- served solves (continuous batching) -------------------------------- */
 

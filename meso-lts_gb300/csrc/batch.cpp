@@ -101,6 +101,42 @@ int launch(meso_batch *b) {
     return MESO_OK;
 }
 
+// Members whose run state or parameters changed since the last upload: rebuild the work list.
+int refresh(meso_batch *b) {
+    bool stale = false;
+    for (size_t i = 0; i < b->members.size(); ++i) {
+        meso_ctx *c = b->members[i];
+        if (!c) continue;
+        cudaStreamSynchronize(c->stream);
+        stale = stale || b->active[i] != (running(c) ? 1 : 0) || b->version[i] != c->f32_version;
+    }
+    return stale ? rebuild(b) : MESO_OK;
+}
+
+// After the steps of one call: the members' step, solution time, run state and residuals.
+int finish(meso_batch *b, const std::vector<int> &start, int32_t *nrunning) {
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess)
+        return fail(MESO_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString(cudaGetLastError()));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    b->last_ms = ms;
+    int still = 0;
+    for (size_t i = 0; i < b->members.size(); ++i) {
+        meso_ctx *c = b->members[i];
+        if (!c || !b->active[i]) continue;
+        int rc = meso_host::ctx_read_status(c);
+        if (rc) return rc;
+        const int done = c->h_status->step - start[i];
+        for (int k = 0; k < done; ++k) c->solution_time += c->params.dt;  // as do_step accumulates it
+        c->step = c->h_status->step;
+        if ((rc = meso_host::ctx_read_resid(c))) return rc;
+        if (c->h_status->stop_step != INT_MAX || c->h_status->timeout) c->run_state = 0;
+        still += running(c) ? 1 : 0;
+    }
+    if (nrunning) *nrunning = still;
+    return MESO_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -166,15 +202,8 @@ int meso_batch_step(meso_batch *b, int32_t nsteps, int32_t *nrunning) {
     if (nsteps < 0) return fail(MESO_ERR_INVALID, "nsteps must be >= 0");
     if (cudaSetDevice(b->device) != cudaSuccess) return fail(MESO_ERR_CUDA, "cannot select the batch's device");
     const int n = (int)b->members.size();
-    bool stale = false;
-    for (int i = 0; i < n; ++i) {
-        meso_ctx *c = b->members[i];
-        if (!c) continue;
-        cudaStreamSynchronize(c->stream);
-        stale = stale || b->active[i] != (running(c) ? 1 : 0) || b->version[i] != c->f32_version;
-    }
-    int rc = MESO_OK;
-    if (stale && (rc = rebuild(b))) return rc;
+    int rc = refresh(b);
+    if (rc) return rc;
     std::vector<int> start(n);
     for (int i = 0; i < n; ++i) start[i] = b->members[i] ? b->members[i]->step : 0;
     b->last_launches = 0;
@@ -187,25 +216,45 @@ int meso_batch_step(meso_batch *b, int32_t nsteps, int32_t *nrunning) {
     for (int it = 0; it < nsteps && nact > 0; ++it)
         if ((rc = launch(b))) return rc;
     cudaEventRecord(b->ev1, b->stream);
-    if (cudaStreamSynchronize(b->stream) != cudaSuccess)
-        return fail(MESO_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString(cudaGetLastError()));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
-    b->last_ms = ms;
-    int still = 0;
-    for (int i = 0; i < n; ++i) {
-        meso_ctx *c = b->members[i];
-        if (!c || !b->active[i]) continue;
-        if ((rc = meso_host::ctx_read_status(c))) return rc;
-        const int done = c->h_status->step - start[i];
-        for (int k = 0; k < done; ++k) c->solution_time += c->params.dt;  // as do_step accumulates it
-        c->step = c->h_status->step;
-        if ((rc = meso_host::ctx_read_resid(c))) return rc;
-        if (c->h_status->stop_step != INT_MAX || c->h_status->timeout) c->run_state = 0;
-        still += running(c) ? 1 : 0;
+    return finish(b, start, nrunning);
+}
+
+int meso_batch_phase_times(meso_batch *b, int32_t nsteps, double *ms, int32_t max_phases, int32_t *nphases) {
+    if (!b) return fail(MESO_ERR_INVALID, "null batch");
+    if (nsteps <= 0 || !ms) return fail(MESO_ERR_INVALID, "nsteps must be > 0 and ms non-null");
+    if (cudaSetDevice(b->device) != cudaSuccess) return fail(MESO_ERR_CUDA, "cannot select the batch's device");
+    int rc = refresh(b);
+    if (rc) return rc;
+    const int np = meso::F32_NPHASE;
+    if (nphases) *nphases = np;
+    const int n = (int)b->members.size();
+    std::vector<int> start(n);
+    for (int i = 0; i < n; ++i) start[i] = b->members[i] ? b->members[i]->step : 0;
+    std::vector<cudaEvent_t> ev((size_t)np + 1);
+    for (auto &e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return fail(MESO_ERR_CUDA, "cannot create the phase events");
+    std::vector<double> acc(np, 0.0);
+    b->last_launches = 0;
+    int nact = 0;
+    for (int i = 0; i < n; ++i) nact += b->active[i] && running(b->members[i]);
+    cudaEventRecord(b->ev0, b->stream);
+    for (int s = 0; s < nsteps && nact > 0 && rc == MESO_OK; ++s) {
+        if (meso::fp32_step(b->fs, b->stream, &b->last_launches, ev.data()) ||
+            cudaEventSynchronize(ev[np]) != cudaSuccess) {
+            rc = fail(MESO_ERR_CUDA, std::string("batch phase timing: ") + cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        for (int k = 0; k < np; ++k) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            acc[k] += t;
+        }
     }
-    if (nrunning) *nrunning = still;
-    return MESO_OK;
+    cudaEventRecord(b->ev1, b->stream);
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (rc) return rc;
+    for (int k = 0; k < np && k < max_phases; ++k) ms[k] = acc[k] / nsteps;
+    return finish(b, start, nullptr);
 }
 
 double meso_batch_last_step_ms(meso_batch *b) { return b ? b->last_ms : 0.0; }

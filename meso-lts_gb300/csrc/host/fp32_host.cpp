@@ -262,6 +262,18 @@ int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso
     });
     int n2 = 0;
     for (const int2 &it : items) n2 += insts[it.x].vpl == 2 ? 1 : 0;
+    // boundary faces: one block per face for large velocity sets, eight faces (a warp each) per
+    // block for small ones
+    std::vector<int2> bblocks;
+    for (int i = 0; i < n; ++i) {
+        const auto &I = insts[i];
+        if (I.NVp <= meso::F32_SMALL_NVP) s.has_small = 1;
+        else s.has_large = 1;
+        if (I.NVp <= meso::F32_SMALL_NVP)
+            for (int b = 0; b < I.nb; b += 8) bblocks.push_back(make_int2(i, -b - 1));
+        else
+            for (int b = 0; b < I.nb; ++b) bblocks.push_back(make_int2(i, b));
+    }
     auto put = [&](const void *src, size_t bytes) -> void * {
         void *p = nullptr;
         if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) return nullptr;
@@ -274,7 +286,10 @@ int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso
     s.d_face_items = (int *)put(foff.data(), sizeof(int) * foff.size());
     s.d_cell_items = (int *)put(coff.data(), sizeof(int) * coff.size());
     s.d_bnd_items = (int *)put(boff.data(), sizeof(int) * boff.size());
-    if (!s.d_inst || !s.d_items || !s.d_face_items || !s.d_cell_items || !s.d_bnd_items) return -1;
+    s.d_bnd_blocks = (int2 *)put(bblocks.data(), sizeof(int2) * bblocks.size());
+    if (!s.d_inst || !s.d_items || !s.d_face_items || !s.d_cell_items || !s.d_bnd_items || !s.d_bnd_blocks)
+        return -1;
+    s.nbnd_blocks = (int)bblocks.size();
     s.ninst = n;
     s.nitems = (int)items.size();
     s.nitems_vpl2 = n2;

@@ -184,6 +184,25 @@ template <int N> __device__ __forceinline__ void warp_sum(float (&v)[N]) {
         for (int k = 0; k < N; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
 }
 
+// Warp sum of per-lane values hi + lo (a compensated FP32 partial: hi = Kahan sum, lo = minus its
+// compensation) as an unevaluated float pair: each xor level adds the partner's pair with Knuth's
+// two-sum (exact rounding error of hi + hi') and renormalises, so the result carries about 44
+// significant bits (the pair's precision) at FP32 instruction rates.  Every lane receives the
+// same, order-independent-of-lane value; the FP64 result is hi + lo.
+__device__ __forceinline__ double warp_sum_ff(float hi, float lo) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float bh = __shfl_xor_sync(0xffffffffu, hi, o), bl = __shfl_xor_sync(0xffffffffu, lo, o);
+        const float sum = __fadd_rn(hi, bh);
+        const float bv = __fsub_rn(sum, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bv)), __fsub_rn(bh, bv));
+        const float l = __fadd_rn(__fadd_rn(lo, bl), err);
+        hi = __fadd_rn(sum, l);
+        lo = __fsub_rn(l, __fsub_rn(hi, sum));
+    }
+    return (double)hi + (double)lo;
+}
+
 template <int N> __device__ __forceinline__ float pick(const float (&v)[N], int lane) {
     float r = 0.f;
 #pragma unroll
@@ -356,13 +375,21 @@ __device__ __forceinline__ float2 recon(const TileSmem<VPL> &sm, int buf, int s,
     return make_float2(fmaf(ax, g.x, fmaf(ay, g.y, x.x)), fmaf(ax, g.z, fmaf(ay, g.w, x.y)));
 }
 
+// The upwind side is selected per lane (slot and offset), so lanes of one warp that upwind from
+// different sides of the face share one reconstruction; only the rare between-sides case (|n.xi|
+// below VSMALL) evaluates the second side.
 template <int VPL>
 __device__ __forceinline__ float2 face_bar(const TileSmem<VPL> &sm, int buf, int v, int cls, int os, int ns,
                                            float2 fdo, float2 fdn, float hx, float hy) {
-    if (cls == 0) return recon(sm, buf, os, v, fdo, hx, hy);
-    if (cls == 1) return recon(sm, buf, ns, v, fdn, hx, hy);
-    const float2 a = recon(sm, buf, os, v, fdo, hx, hy), b = recon(sm, buf, ns, v, fdn, hx, hy);
-    return make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
+    const bool nb = cls == 1;
+    const int s = nb ? ns : os;
+    const float2 d = make_float2(nb ? fdn.x : fdo.x, nb ? fdn.y : fdo.y);
+    float2 a = recon(sm, buf, s, v, d, hx, hy);
+    if (cls == 2) {
+        const float2 b = recon(sm, buf, ns, v, fdn, hx, hy);
+        a = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
+    }
+    return a;
 }
 
 
@@ -601,6 +628,11 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
 // =============================================================================
 // FMa: face moments from the stored reconstructions (one warp per face), face macros in FP64
 // =============================================================================
+// Two forms, each launched over the faces of the instances of its class: large velocity sets
+// (NVp > F32_SMALL_NVP: long streaming loops, blocks of 4 velocities per lane, FP64 warp sums) and
+// small ones (blocks of 8, float-float warp sums, which cost a fraction of the FP64 pipe time
+// that dominates short faces).
+template <int NB, bool SMALL>
 __global__ void __launch_bounds__(256) k32_face_moments(const F32Inst *__restrict__ insts, const int *__restrict__ foff,
                                                        int ninst, int total) {
     const int lane = threadIdx.x & 31;
@@ -608,23 +640,23 @@ __global__ void __launch_bounds__(256) k32_face_moments(const F32Inst *__restric
     for (int g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
         const int i = find_inst(foff, ninst, g);
         const F32Inst &I = insts[i];
-        if (step_stopped(I.status)) continue;
+        if (step_stopped(I.status) || (I.NVp <= F32_SMALL_NVP) != SMALL) continue;
         const int f = g - foff[i];
         const float2 uo = I.u32[I.fown[f]], un = I.u32[I.fnei[f]];
         const float u0xf = 0.5f * (uo.x + un.x), u0yf = 0.5f * (uo.y + un.y);
         // 11 raw moments about u0 of the face's reconstructed deviations (cdugks_shakhov.cpp:305-349):
-        // FP32 terms summed over blocks of 4 velocities per lane, compensated across blocks
+        // FP32 terms summed over blocks of NB velocities per lane, compensated across blocks
         const int b = I.fbnd[f];
         const float2 *__restrict__ src = b >= 0 ? I.bnd_in + (size_t)b * I.NVp : I.fbar + (size_t)f * I.NVp;
         const float4 *__restrict__ vt32 = I.vt32;
         float s[F32_NMOM], c[F32_NMOM];
 #pragma unroll
         for (int k = 0; k < F32_NMOM; ++k) s[k] = c[k] = 0.f;
-        for (int p0 = 0; p0 < I.NVp; p0 += 32 * 4) {
-            float4 tv[4];
-            float2 gv[4];
+        for (int p0 = 0; p0 < I.NVp; p0 += 32 * NB) {
+            float4 tv[NB];
+            float2 gv[NB];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
+            for (int j = 0; j < NB; ++j) {
                 const int p = p0 + 32 * j + lane;
                 tv[j] = p < I.NVp ? vt32[p] : make_float4(0.f, 0.f, 0.f, 0.f);
                 gv[j] = p < I.NVp ? src[p] : make_float2(0.f, 0.f);
@@ -633,7 +665,7 @@ __global__ void __launch_bounds__(256) k32_face_moments(const F32Inst *__restric
 #pragma unroll
             for (int k = 0; k < F32_NMOM; ++k) m[k] = 0.f;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
+            for (int j = 0; j < NB; ++j) {
                 const float c0x = tv[j].x - u0xf, c0y = tv[j].y - u0yf;
                 const float wg = tv[j].z * gv[j].x, wh = tv[j].z * gv[j].y;
                 const float cc = fmaf(c0x, c0x, c0y * c0y);
@@ -656,10 +688,14 @@ __global__ void __launch_bounds__(256) k32_face_moments(const F32Inst *__restric
         double M[F32_NMOM];
 #pragma unroll
         for (int k = 0; k < F32_NMOM; ++k) {
-            double v = (double)s[k] - (double)c[k];
+            if (SMALL) {
+                M[k] = warp_sum_ff(s[k], -c[k]);
+            } else {
+                double v = (double)s[k] - (double)c[k];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            M[k] = v;
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                M[k] = v;
+            }
         }
         if (lane < F32_NMOM) {
             double mine = M[0];
@@ -802,7 +838,8 @@ __global__ void __launch_bounds__(256) k32_face_eqflux(const F32Inst *__restrict
 }
 
 // =============================================================================
-// BND: boundary faces (one block per face); cdugks_shakhov.cpp:364-607
+// BND: boundary faces; cdugks_shakhov.cpp:364-607.  A group of TPF threads per face: the block
+// (TPF = 256) for large velocity sets, one warp (TPF = 32, eight faces per block) for small ones.
 // =============================================================================
 __device__ __forceinline__ double block_sum(double v, double *sh) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -821,41 +858,86 @@ __device__ __forceinline__ double solve_pressure(double P0, double R, double T, 
     return P0 / pow(1.0 + (gamma - 1.0) / 2.0 * (Ma * Ma), gamma / (gamma - 1.0));
 }
 
-__global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ insts, const int *__restrict__ boff,
-                                                   int ninst, int total) {
-    __shared__ double sh[8];
-    for (int g = blockIdx.x; g < total; g += gridDim.x) {
-        const int i = find_inst(boff, ninst, g);
-        const F32Inst &I = insts[i];
-        if (step_stopped(I.status)) continue;
-        const int b = g - boff[i];
-        const int f = I.bface[b];
-        const meso_mark_desc mk = I.marks[I.fmark[f]];
-        const int nb = I.fown[f];
+constexpr int kBndThreads = 256;
+
+// Per-face scalars the group shares (written by its first warp).
+struct BndShared {
+    EqP ew, ein;
+    double red[kBndThreads / 32][4];
+    double tot[4];
+    double rr, TT, uux, uuy;
+    int mode;
+};
+
+template <int TPF> struct BndGroup;
+template <> struct BndGroup<32> {  // one warp per face
+    static __device__ __forceinline__ int rank() { return threadIdx.x & 31; }
+    static __device__ __forceinline__ bool leader() { return true; }
+    static __device__ __forceinline__ void sync() { __syncwarp(); }
+};
+template <> struct BndGroup<kBndThreads> {  // the block per face
+    static __device__ __forceinline__ int rank() { return threadIdx.x; }
+    static __device__ __forceinline__ bool leader() { return threadIdx.x < 32; }
+    static __device__ __forceinline__ void sync() { __syncthreads(); }
+};
+
+// Group sums of N compensated FP32 partials (sum s, compensation c) in float-float, then FP64
+// across the block's warps in warp order; every thread of the group receives the totals.
+template <int TPF, int N>
+__device__ __forceinline__ void group_sum(const float (&s)[N], const float (&c)[N], double (&out)[N], BndShared &S) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) out[k] = warp_sum_ff(s[k], -c[k]);
+    if (TPF == 32) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < N; ++k) S.red[warp][k] = out[k];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            double v = lane < kBndThreads / 32 ? S.red[lane][k] : 0.0;
+#pragma unroll
+            for (int o = kBndThreads / 64; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) S.tot[k] = v;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; ++k) out[k] = S.tot[k];
+}
+
+template <int TPF> __device__ __forceinline__ void bnd_face(const F32Inst &I, int b, BndShared &S) {
+    using G = BndGroup<TPF>;
+    const int r = G::rank();
+    const int f = I.bface[b];
+    const meso_mark_desc &mk = I.marks[I.fmark[f]];
+    const int nb = I.fown[f];
+    const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
+    float2 *bin = I.bnd_in + (size_t)b * I.NVp;
+    float2 *bout = I.bnd_out + (size_t)b * I.NVp;
+    const float2 n = I.fn32[f];
+    const double2 n64 = I.fn64[f];
+    {  // blend with the face equilibrium (cdugks_shakhov.cpp:350-361), deviations from (g0, h0)
         const FaceK k = I.fk[f];
-        const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
-        float2 *bin = I.bnd_in + (size_t)b * I.NVp;
-        float2 *bout = I.bnd_out + (size_t)b * I.NVp;
-        const float2 n = I.fn32[f];
-        const double2 n64 = I.fn64[f];
-        // blend with the face equilibrium (cdugks_shakhov.cpp:350-361), deviations from (g0, h0)
-        for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
-            const float xx = I.xi32x[p], xy = I.xi32y[p];
-            const float2 gs = dshakhov(k.e, xx, xy, fmaf(xx, xx, xy * xy), I.g0_32[p], k3, twoK);
+        for (int p = r; p < I.NVp; p += TPF) {
+            const float4 t = I.vt32[p];
+            const float2 gs = dshakhov(k.e, t.x, t.y, fmaf(t.x, t.x, t.y * t.y), t.w, k3, twoK);
             const float2 gb = bin[p];
             bin[p] = make_float2(fmaf(k.oCs, gb.x, k.Cs * gs.x), fmaf(k.oCs, gb.y, k.Cs * gs.y));
         }
-        __syncthreads();
-        // incoming set for this face type; kn = xi . n_in = -(xi . n0): class 1 = incoming, 2 = grazing
+    }
+    // incoming set for this face type; kn = xi . n_in = -(xi . n0): class 1 = incoming, 2 = grazing
+    if (G::leader()) {
         const int type = mk.type;
         double rr = 0.0, TT = 0.0, uux = 0.0, uuy = 0.0;
         int mode = 0;  // 0 keep, 1 Maxwell incoming, 2 wall, 3 slip wall, 4 symmetry
         if (type == MESO_BC_PRESSURE_INLET) {
             const double T_m = I.T[nb], umx = I.u[3 * nb], umy = I.u[3 * nb + 1];
             const double nx = -n64.x, ny = -n64.y;
-            const double s = umx * nx + umy * ny;
-            uux = nx * s;
-            uuy = ny * s;
+            const double sn = umx * nx + umy * ny;
+            uux = nx * sn;
+            uuy = ny * sn;
             TT = mk.temperature;
             rr = solve_pressure(mk.pressure, I.R, T_m, uux, uuy, I.gamma) / (I.R * TT);
             mode = 1;
@@ -875,9 +957,9 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
             const double umx = I.u[3 * nb], umy = I.u[3 * nb + 1], T_m = I.T[nb];
             rr = solve_pressure(mk.pressure, I.R, T_m, umx, umy, I.gamma) / (I.R * T_m);
             const double nx = n64.x, ny = n64.y;  // nv_e = -nv = n0
-            const double s = umx * nx + umy * ny;
-            uux = nx * s;
-            uuy = ny * s;
+            const double sn = umx * nx + umy * ny;
+            uux = nx * sn;
+            uuy = ny * sn;
             TT = mk.temperature;
             mode = 1;
         } else if (type == MESO_BC_FARFIELD_OUTLET) {
@@ -893,93 +975,136 @@ __global__ void __launch_bounds__(256) k32_boundary(const F32Inst *__restrict__ 
         } else if (type == MESO_BC_SYMMETRY) {
             mode = 4;
         }
-        double rho_w = 0.0, den_w = 0.0;
         if (mode == 2 || mode == 3) {
-            // diffuse-wall density balance (cdugks_shakhov.cpp:468-497): outgoing mass of the
-            // blended face values over the incoming mass of a unit-density wall Maxwellian
-            // g0 (1 + expm1(E_w)); the g0 parts are the precomputed half-range sums
+            // the balance's wall Maxwellian: zeroGradient walls balance with the cell's temperature
             double T_w = 0.0;
             if (mk.temperature_type == MESO_PATCH_ZERO_GRADIENT) T_w = I.T[nb];
             else if (mk.temperature_type == MESO_PATCH_FIXED_VALUE) T_w = mk.temperature;
             const EqP ew = make_eqp(I, 1.0, mk.velocity[0], mk.velocity[1], T_w, 0.0, 0.0);
-            float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
-            for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
-                const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
-                const float d = fmaf(n.x, xx, n.y * xy);
-                const int cls = classify(I, f, p, d, xx, xy);
-                if (cls == 1) {  // kn = -d >= VSMALL
-                    const float E = fmaf(ew.ea, fmaf(xx, xx, xy * xy), fmaf(ew.ebx, xx, fmaf(ew.eby, xy, ew.ec)));
-                    kahan(s1, c1, -d * w * I.g0_32[p] * expm1_dev(E));
-                } else {
-                    kahan(s0, c0, d * w * bin[p].x);
-                }
-            }
-            const double num = I.bnd_g0[2 * b] + block_sum((double)s0 - (double)c0, sh);
-            const double den = I.bnd_g0[2 * b + 1] + block_sum((double)s1 - (double)c1, sh);
-            rho_w = num / den;
-            den_w = den;
-            rr = rho_w;
-            TT = mk.temperature;
-            uux = mk.velocity[0];
-            uuy = mk.velocity[1];
+            if ((threadIdx.x & 31) == 0) S.ew = ew;
         }
-        // incoming Maxwellian (rr, uu, TT) as a deviation from (g0, h0)
-        const EqP ein = make_eqp(I, rr > 0.0 ? rr : 1.0, uux, uuy, TT > 0.0 ? TT : I.T0, 0.0, 0.0);
-        const int dir = mk.direction;
-        const float au = (float)mk.alpha_u, aT = (float)mk.alpha_T;
-        // The balance and the incoming set use the same temperature only for a fixedValue wall
-        // (a zeroGradient wall balances with T_cell but sets with the patch scalar, :473-479 vs :533).
-        const bool exact_mass = mode == 2 && mk.temperature_type == MESO_PATCH_FIXED_VALUE;
-        float sm4[4] = {0.f, 0.f, 0.f, 0.f}, cm4[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
-            const float xx = I.xi32x[p], xy = I.xi32y[p], w = I.w32[p];
+        if ((threadIdx.x & 31) == 0) {
+            S.mode = mode;
+            S.rr = rr;
+            S.TT = TT;
+            S.uux = uux;
+            S.uuy = uuy;
+        }
+    }
+    G::sync();  // blended values and the face scalars are visible to the whole group
+    const int mode = S.mode;
+    double rr = S.rr, TT = S.TT, uux = S.uux, uuy = S.uuy;
+    double rho_w = 0.0, den_w = 0.0;
+    if (mode == 2 || mode == 3) {
+        // diffuse-wall density balance (cdugks_shakhov.cpp:468-497): outgoing mass of the
+        // blended face values over the incoming mass of a unit-density wall Maxwellian
+        // g0 (1 + expm1(E_w)); the g0 parts are the precomputed half-range sums
+        const EqP ew = S.ew;
+        float s2[2] = {0.f, 0.f}, c2[2] = {0.f, 0.f};
+        for (int p = r; p < I.NVp; p += TPF) {
+            const float4 t = I.vt32[p];
+            const float xx = t.x, xy = t.y, w = t.z;
             const float d = fmaf(n.x, xx, n.y * xy);
-            float2 v = bin[p];
-            int cls = 0;
-            if (mode != 0 && p < I.NV) {
-                cls = classify(I, f, p, d, xx, xy);
-                if (mode == 4) {
-                    const float2 r = bin[I.sym[3 * p + dir]];
-                    if (cls == 1) v = r;
-                    else if (cls == 2) v = make_float2(0.5f * (v.x + r.x), 0.5f * (v.y + r.y));
-                } else if (cls != 0) {
-                    float2 inc = dshakhov(ein, xx, xy, fmaf(xx, xx, xy * xy), I.g0_32[p], k3, twoK);
-                    if (mode == 3) {
-                        const float2 r = bin[I.sym[3 * p + dir]];
-                        inc = make_float2((1.f - au) * inc.x + au * r.x, (1.f - aT) * inc.y + aT * r.y);
-                    }
-                    if (mode == 1) {
-                        if (cls == 1) v = inc;
-                    } else {
-                        v = cls == 1 ? inc : make_float2(0.5f * (inc.x + v.x), 0.5f * (inc.y + v.y));
-                    }
+            const int cls = classify(I, f, p, d, xx, xy);
+            if (cls == 1) {  // kn = -d >= VSMALL
+                const float E = fmaf(ew.ea, fmaf(xx, xx, xy * xy), fmaf(ew.ebx, xx, fmaf(ew.eby, xy, ew.ec)));
+                kahan(s2[1], c2[1], -d * w * t.w * expm1_dev(E));
+            } else {
+                kahan(s2[0], c2[0], d * w * bin[p].x);
+            }
+        }
+        double tot2[2];
+        group_sum<TPF, 2>(s2, c2, tot2, S);
+        const double num = I.bnd_g0[2 * b] + tot2[0];
+        const double den = I.bnd_g0[2 * b + 1] + tot2[1];
+        rho_w = num / den;
+        den_w = den;
+        rr = rho_w;
+        TT = mk.temperature;
+        uux = mk.velocity[0];
+        uuy = mk.velocity[1];
+    }
+    // incoming Maxwellian (rr, uu, TT) as a deviation from (g0, h0)
+    if (G::leader()) {
+        const EqP ein = make_eqp(I, rr > 0.0 ? rr : 1.0, uux, uuy, TT > 0.0 ? TT : I.T0, 0.0, 0.0);
+        if ((threadIdx.x & 31) == 0) S.ein = ein;
+    }
+    G::sync();
+    const EqP ein = S.ein;
+    const int dir = mk.direction;
+    const float au = (float)mk.alpha_u, aT = (float)mk.alpha_T;
+    // The balance and the incoming set use the same temperature only for a fixedValue wall
+    // (a zeroGradient wall balances with T_cell but sets with the patch scalar, :473-479 vs :533).
+    const bool exact_mass = mode == 2 && mk.temperature_type == MESO_PATCH_FIXED_VALUE;
+    const float knA0 = I.farea[f];
+    float sm4[4] = {0.f, 0.f, 0.f, 0.f}, cm4[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int p = r; p < I.NVp; p += TPF) {
+        const float4 t = I.vt32[p];
+        const float xx = t.x, xy = t.y, w = t.z;
+        const float d = fmaf(n.x, xx, n.y * xy);
+        float2 v = bin[p];
+        int cls = 0;
+        if (mode != 0 && p < I.NV) {
+            cls = classify(I, f, p, d, xx, xy);
+            if (mode == 4) {
+                const float2 rv = bin[I.sym[3 * p + dir]];
+                if (cls == 1) v = rv;
+                else if (cls == 2) v = make_float2(0.5f * (v.x + rv.x), 0.5f * (v.y + rv.y));
+            } else if (cls != 0) {
+                float2 inc = dshakhov(ein, xx, xy, fmaf(xx, xx, xy * xy), t.w, k3, twoK);
+                if (mode == 3) {
+                    const float2 rv = bin[I.sym[3 * p + dir]];
+                    inc = make_float2((1.f - au) * inc.x + au * rv.x, (1.f - aT) * inc.y + aT * rv.y);
+                }
+                if (mode == 1) {
+                    if (cls == 1) v = inc;
+                } else {
+                    v = cls == 1 ? inc : make_float2(0.5f * (inc.x + v.x), 0.5f * (inc.y + v.y));
                 }
             }
-            // the face's flux value (n0.xi) A f for the update kernel
-            const float knA = d * I.farea[f];
-            bout[p] = make_float2(knA * v.x, knA * v.y);
-            // moment fluxes of the deviations along n0 (the g0 parts are added in FP64 below)
-            const float wkn = w * d;
-            const float a = wkn * v.x;
-            // diffuse wall: the incoming mass flux is rho_w * den exactly (added below), so the face
-            // carries no net mass in FP32 storage either (cdugks_shakhov.cpp:468-497)
-            if (!(exact_mass && cls == 1)) kahan(sm4[0], cm4[0], a);
-            kahan(sm4[1], cm4[1], a * xx);
-            kahan(sm4[2], cm4[2], a * xy);
-            kahan(sm4[3], cm4[3], wkn * fmaf(fmaf(xx, xx, xy * xy), v.x, v.y));
         }
-        double tot[4];
-        for (int q = 0; q < 4; ++q) tot[q] = block_sum((double)sm4[q] - (double)cm4[q], sh);
+        // the face's flux value (n0.xi) A f for the update kernel
+        const float knA = d * knA0;
+        bout[p] = make_float2(knA * v.x, knA * v.y);
+        // moment fluxes of the deviations along n0 (the g0 parts are added in FP64 below)
+        const float wkn = w * d;
+        const float a = wkn * v.x;
+        // diffuse wall: the incoming mass flux is rho_w * den exactly (added below), so the face
+        // carries no net mass in FP32 storage either (cdugks_shakhov.cpp:468-497)
+        if (!(exact_mass && cls == 1)) kahan(sm4[0], cm4[0], a);
+        kahan(sm4[1], cm4[1], a * xx);
+        kahan(sm4[2], cm4[2], a * xy);
+        kahan(sm4[3], cm4[3], wkn * fmaf(fmaf(xx, xx, xy * xy), v.x, v.y));
+    }
+    double tot[4];
+    group_sum<TPF, 4>(sm4, cm4, tot, S);
+    if (r == 0) {
         double g0f[4];
         g0_fluxes(I, n64.x, n64.y, g0f);
         // exact-mass wall: the g0 mass over the non-incoming set is the balance's numerator part
         tot[0] += exact_mass ? I.bnd_g0[2 * b] - rho_w * den_w : g0f[0];
         for (int q = 1; q < 4; ++q) tot[q] += g0f[q];
-        if (threadIdx.x == 0) {
-            double *o = I.fsum + (size_t)f * 4;
-            for (int q = 0; q < 4; ++q) o[q] = tot[q];
+        double *o = I.fsum + (size_t)f * 4;
+        for (int q = 0; q < 4; ++q) o[q] = tot[q];
+    }
+    G::sync();  // the group's shared scalars are rewritten by its next face
+}
+
+// Work items (instance, first boundary face): y >= 0 is one face for the whole block, y < 0 is
+// the eight faces -y - 1 ... -y + 6 of the instance, one per warp.
+__global__ void __launch_bounds__(kBndThreads) k32_boundary(const F32Inst *__restrict__ insts,
+                                                           const int2 *__restrict__ items, int nitems) {
+    __shared__ BndShared sh[kBndThreads / 32];
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int2 item = items[it];
+        const F32Inst &I = insts[item.x];
+        if (step_stopped(I.status)) continue;
+        if (item.y >= 0) {
+            bnd_face<kBndThreads>(I, item.y, sh[0]);
+        } else {
+            const int b = -item.y - 1 + (threadIdx.x >> 5);
+            if (b < I.nb) bnd_face<32>(I, b, sh[threadIdx.x >> 5]);
         }
-        __syncthreads();
     }
 }
 
@@ -1364,8 +1489,13 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     mark(0);
     tiles(false);
     mark(1);
-    k32_face_moments<<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
-                                                                         s.total_faces);
+    if (s.has_large)
+        k32_face_moments<4, false><<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items,
+                                                                                   s.ninst, s.total_faces);
+    if (s.has_small)
+        k32_face_moments<8, true><<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items,
+                                                                                  s.ninst, s.total_faces);
+    n += (s.has_large ? 1 : 0) + (s.has_small ? 1 : 0) - 1;
     k32_face_macros<<<grid_of(s.total_faces, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
                                                                           s.total_faces);
     mark(2);
@@ -1373,8 +1503,8 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     if (branch) {  // boundary faces on the side stream, interior faces' equilibrium fluxes here
         cudaEventRecord(fork->fork, stream);
         cudaStreamWaitEvent(fork->side, fork->fork, 0);
-        k32_boundary<<<grid_of(s.total_bnd, 1, cap), 256, 0, fork->side>>>(s.d_inst, s.d_bnd_items, s.ninst,
-                                                                           s.total_bnd);
+        k32_boundary<<<grid_of(s.nbnd_blocks, 1, cap), kBndThreads, 0, fork->side>>>(s.d_inst, s.d_bnd_blocks,
+                                                                                     s.nbnd_blocks);
         cudaEventRecord(fork->join, fork->side);
     }
     k32_face_eqflux<<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
@@ -1385,7 +1515,8 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
         cudaStreamWaitEvent(stream, fork->join, 0);
         ++n;
     } else if (s.total_bnd > 0) {
-        k32_boundary<<<grid_of(s.total_bnd, 1, cap), 256, 0, stream>>>(s.d_inst, s.d_bnd_items, s.ninst, s.total_bnd);
+        k32_boundary<<<grid_of(s.nbnd_blocks, 1, cap), kBndThreads, 0, stream>>>(s.d_inst, s.d_bnd_blocks,
+                                                                                 s.nbnd_blocks);
         ++n;
     }
     mark(4);

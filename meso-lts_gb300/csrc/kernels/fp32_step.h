@@ -25,6 +25,7 @@ constexpr int F32_DEFAULT_CELLS = 48;  // tile size without an autotuned shape (
 constexpr int F32_MAX_CF = 200;     // cell-face entries per tile (tile cells x faces per cell)
 constexpr int F32_MAX_TF = 120;     // faces touching a tile cell (< 128: indices fit 7 bits)
 constexpr int F32_NMOM = 11;        // raw face moments about the reference velocity (2-D)
+constexpr int F32_SMALL_NVP = 2048;  // velocity sets up to this size: a warp per boundary face, float-float face sums
 
 // Scalars of one Shakhov equilibrium (rho, u, T, q) for FP32 evaluation of its
 // deviation from the instance's reference Maxwellian g0 (see F32Inst::g0_32):
@@ -134,6 +135,9 @@ struct Fp32State {
     int *d_face_items = nullptr; // prefix sums of faces / cells / boundary faces over instances
     int *d_cell_items = nullptr;
     int *d_bnd_items = nullptr;
+    int2 *d_bnd_blocks = nullptr; // boundary-kernel blocks: (inst, face b) or (inst, -(first of 8 faces) - 1)
+    int nbnd_blocks = 0;
+    int has_small = 0, has_large = 0;  // instances with NVp <= / > F32_SMALL_NVP
     int total_faces = 0, total_cells = 0, total_bnd = 0;
     int num_sms = 0;
 };

@@ -113,6 +113,7 @@ _SIGS = {
     "meso_batch_size": (C.c_int32, [C.c_void_p]),
     "meso_batch_last_step_ms": (C.c_double, [C.c_void_p]),
     "meso_batch_last_step_launches": (C.c_int64, [C.c_void_p]),
+    "meso_batch_phase_times": (C.c_int, [C.c_void_p, C.c_int32, _dp, C.c_int32, _ip]),
     "meso_autotune": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(DvsDesc), C.POINTER(MarkDesc), C.c_int32,
                                  C.POINTER(Params), C.c_int32, C.POINTER(Params), _dp]),
     "meso_autotune_case": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(Params), _dp]),
@@ -366,6 +367,14 @@ class Batch:
 
     def last_step_launches(self) -> int:
         return lib().meso_batch_last_step_launches(self._h)
+
+    def phase_times(self, nsteps: int = 3) -> dict:
+        """Mean device ms per step of each phase, kernels launched one by one (steps the batch)."""
+        ms = np.zeros(16)
+        n = C.c_int32()
+        _check(lib().meso_batch_phase_times(self._h, nsteps, _ptr(ms), 16, C.byref(n)))
+        names = [lib().meso_phase_name(self.solvers[0].handle, i).decode() for i in range(n.value)]
+        return dict(zip(names, ms[: n.value].tolist()))
 
     def close(self):
         if self._h:
