@@ -64,10 +64,21 @@ __device__ __forceinline__ float fast_ex2(float x) {
     return y;
 }
 
+// True when both products of n0.xi have a zero factor in FP32 and |xi_x| + |xi_y| < 1e7 (margin
+// < 100).  The FP64 factors are then zero or below the FP32 normal range (1.2e-38), so |n0.xi| <
+// 1.2e-31 < VSMALL = 1e-30 in FP64 as well: the velocity lies between the sides (class 2) without
+// an FP64 evaluation.  This is the grazing set of axis-aligned faces (uniform meshes, walls) and
+// of velocity sets with zero components.
+__device__ __forceinline__ bool zero_products(float nx, float ny, float xx, float xy, float margin) {
+    return (nx == 0.f || xx == 0.f) && (ny == 0.f || xy == 0.f) && margin < 100.f;
+}
+
 // The same with the face's FP64 normal and the velocity's FP64 components already at hand.
-__device__ __forceinline__ int classify_r(double2 n, double x64, double y64, float d32, float margin) {
+__device__ __forceinline__ int classify_r(double2 n, float2 n32, float xx, float xy, double x64, double y64, float d32,
+                                          float margin) {
     if (d32 > margin) return 0;
     if (d32 < -margin) return 1;
+    if (zero_products(n32.x, n32.y, xx, xy, margin)) return 2;
     const double d = __dadd_rn(__dmul_rn(n.x, x64), __dmul_rn(n.y, y64));
     return d >= kVSMALL ? 0 : (d < -kVSMALL ? 1 : 2);
 }
@@ -77,6 +88,8 @@ __device__ __forceinline__ int classify(const F32Inst &I, int f, int p, float d3
     const float margin = 1e-5f * (fabsf(xx) + fabsf(xy));
     if (d32 > margin) return 0;
     if (d32 < -margin) return 1;
+    const float2 n32 = I.fn32[f];
+    if (zero_products(n32.x, n32.y, xx, xy, margin)) return 2;
     const double2 n = I.fn64[f];
     const double d = __dadd_rn(__dmul_rn(n.x, I.xi64x[p]), __dmul_rn(n.y, I.xi64y[p]));
     return d >= kVSMALL ? 0 : (d < -kVSMALL ? 1 : 2);
@@ -345,7 +358,29 @@ template <int VPL> __device__ __forceinline__ void gradients(TileSmem<VPL> &sm, 
             c[v] = phi[s * SEG + v * 32 + lane];
         }
         if (gradient_on) {
-            for (int j = sm.gptr[s]; j < sm.gptr[s + 1]; ++j) {
+            const int j0 = sm.gptr[s], j1 = sm.gptr[s + 1];
+            int j = j0;
+            for (; j + 4 <= j1; j += 4) {  // four stencil entries: all loads, then the sums in entry order
+                float2 a[4], x[4][VPL];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int nb = sm.gnbr[j + q] * SEG + lane;
+                    a[q] = sm.ga[j + q];
+#pragma unroll
+                    for (int v = 0; v < VPL; ++v) x[q][v] = phi[nb + v * 32];
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int v = 0; v < VPL; ++v) {
+                        const float dg = x[q][v].x - c[v].x, dh = x[q][v].y - c[v].y;
+                        g[v].x = fmaf(a[q].x, dg, g[v].x);
+                        g[v].y = fmaf(a[q].y, dg, g[v].y);
+                        g[v].z = fmaf(a[q].x, dh, g[v].z);
+                        g[v].w = fmaf(a[q].y, dh, g[v].w);
+                    }
+            }
+            for (; j < j1; ++j) {
                 const int nb = sm.gnbr[j] * SEG + lane;
                 const float2 a = sm.ga[j];
 #pragma unroll
@@ -457,6 +492,7 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
                 hx[v] = hdt * xx[v];
                 hy[v] = hdt * xy[v];
             }
+#pragma unroll 2
             for (int fl = warp; fl < nOF; fl += F32_WARPS) {
                 const OwnedFace o = sm.u.p1.of[fl];
                 if (o.bnd >= 0) {  // own = neighbour: every upwind choice gives the owner's reconstruction
@@ -467,7 +503,8 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
                     float2 *dst = fbar + (size_t)o.face * NVp;
 #pragma unroll
                     for (int v = 0; v < VPL; ++v) {
-                        const int cls = classify_r(o.n64, x64[v], y64[v], fmaf(o.n.x, xx[v], o.n.y * xy[v]), mg[v]);
+                        const int cls = classify_r(o.n64, o.n, xx[v], xy[v], x64[v], y64[v],
+                                                   fmaf(o.n.x, xx[v], o.n.y * xy[v]), mg[v]);
                         dst[p[v]] = face_bar(sm, buf, v, cls, o.os, o.ns, o.fdo, o.fdn, hx[v], hy[v]);
                     }
                 }
@@ -569,6 +606,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
 #pragma unroll
                 for (int v = 0; v < VPL; ++v) fg[v] = fh[v] = 0.f;
                 const int e1 = sm.cf_off[cl + 1];
+#pragma unroll 4
                 for (int e = sm.cf_off[cl]; e < e1; ++e) {  // outward flux of the cell (:616-629)
                     const unsigned char t = sm.cft[e];
                     const float2 *ff = sm.fv[buf] + (t & 0x7f) * SEG + lane;
