@@ -507,6 +507,7 @@ int refresh_f32(meso_ctx *c) {
     const meso_params &p = c->params;
     I.dt = p.dt;
     I.hdt = p.dt * 0.5;
+    I.hdt32 = (float)I.hdt;
     I.Pr = p.Pr;
     I.mu0 = p.mu0;
     I.vhs = p.vhs_index;

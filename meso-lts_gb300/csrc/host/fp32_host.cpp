@@ -62,12 +62,15 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
     const meso_params &p = c->params;
     I.dt = p.dt;
     I.hdt = p.dt * 0.5;
+    I.hdt32 = (float)I.hdt;
     I.R = p.R;
     I.Pr = p.Pr;
     I.mu0 = p.mu0;
     I.vhs = p.vhs_index;
     I.T0 = p.T0;
     I.Kd = (double)p.K;
+    I.k3_32 = (float)(I.Kd + 1.0);
+    I.twoK32 = (float)(2.0 * I.Kd);
     I.Cv = (p.K + 3.0) * p.R * 0.5;
     I.gamma = (p.K + 5.0) / (p.K + 3.0);
     I.rho0 = p.rho0 > 0.0 ? p.rho0 : 1.0;
@@ -193,6 +196,7 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.fmac = A.alloc<double>((size_t)F * 8);
         I.fgbar = A.alloc<double>((size_t)F * 4);
         I.fsum = A.alloc<double>((size_t)F * 4);
+        I.g0flux = A.alloc<double>((size_t)F * 4);
         I.bnd_in = A.alloc<float2>((size_t)std::max(I.nb, 1) * NVp);
         I.bnd_out = A.alloc<float2>((size_t)std::max(I.nb, 1) * NVp);
         I.bnd_g0 = A.alloc<double>(2 * (size_t)std::max(I.nb, 1));

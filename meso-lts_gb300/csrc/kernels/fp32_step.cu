@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
         if (ch0 >= ch1) continue;
         const float2 *__restrict__ S = I.S[cur];
         const int NVp = I.NVp;
-        const float hdt = (float)I.hdt;
+        const float hdt = I.hdt32;
         const int grad_on = I.gradient;
         const float4 *__restrict__ vt32 = I.vt32;
         float2 *__restrict__ bnd_in = I.bnd_in;
@@ -553,7 +553,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         const float2 *__restrict__ S = I.S[cur];
         float2 *__restrict__ Sn = I.S[cur ^ 1];
         const int NVp = I.NVp;
-        const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
+        const float k3 = I.k3_32, twoK = I.twoK32;
         const float4 *__restrict__ vt32 = I.vt32;
         const int j0 = I.cf_ptr[cs];
         for (int c = threadIdx.x; c < nc; c += kT) sm.ck[c] = I.ck[cs + c];
@@ -645,15 +645,10 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
             __syncthreads();
         }
 #pragma unroll
-        for (int r = 0; r < RC; ++r) {  // one warp reduction per cell and item, in FP64
+        for (int r = 0; r < RC; ++r) {  // one float-float warp reduction per cell and item
             const int cl = warp + F32_WARPS * r;
             if (cl >= nc) break;
-            double q0 = (double)qs[r][0] - (double)qc[r][0], q1 = (double)qs[r][1] - (double)qc[r][1];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                q0 += __shfl_xor_sync(0xffffffffu, q0, o);
-                q1 += __shfl_xor_sync(0xffffffffu, q1, o);
-            }
+            const double q0 = warp_sum_ff(qs[r][0], -qc[r][0]), q1 = warp_sum_ff(qs[r][1], -qc[r][1]);
             if (lane == 0) {
                 I.qpart[((size_t)grp * I.C + cs + cl) * 2] = q0;
                 I.qpart[((size_t)grp * I.C + cs + cl) * 2 + 1] = q1;
@@ -821,7 +816,7 @@ __global__ void __launch_bounds__(256) k32_face_eqflux(const F32Inst *__restrict
         const FaceK k = I.fk[f];
         const float2 n = I.fn32[f];
         const float area = I.farea[f];
-        const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
+        const float k3 = I.k3_32, twoK = I.twoK32;
         const float4 *__restrict__ vt32 = I.vt32;
         float2 *__restrict__ fb = I.fbar + (size_t)f * I.NVp;
         // plain FP32 sums over blocks of 8 velocities per lane, compensated across blocks; each
@@ -863,14 +858,9 @@ __global__ void __launch_bounds__(256) k32_face_eqflux(const F32Inst *__restrict
         }
         float v[4] = {s[0] - c[0], s[1] - c[1], s[2] - c[2], s[3] - c[3]};
         warp_sum(v);
-        if (lane == 0) {
-            double g0f[4];
-            g0_fluxes(I, I.fn64[f].x, I.fn64[f].y, g0f);
-            double *o = I.fsum + (size_t)f * 4;
-            o[0] = g0f[0] + v[0];
-            o[1] = g0f[1] + v[1];
-            o[2] = g0f[2] + v[2];
-            o[3] = g0f[3] + v[3];
+        if (lane < 4) {
+            const double *g0f = I.g0flux + (size_t)f * 4;
+            I.fsum[(size_t)f * 4 + lane] = g0f[lane] + (double)pick(v, lane);
         }
     }
 }
@@ -951,7 +941,7 @@ template <int TPF> __device__ __forceinline__ void bnd_face(const F32Inst &I, in
     const int f = I.bface[b];
     const meso_mark_desc &mk = I.marks[I.fmark[f]];
     const int nb = I.fown[f];
-    const float k3 = (float)(I.Kd + 1.0), twoK = (float)(2.0 * I.Kd);
+    const float k3 = I.k3_32, twoK = I.twoK32;
     float2 *bin = I.bnd_in + (size_t)b * I.NVp;
     float2 *bout = I.bnd_out + (size_t)b * I.NVp;
     const float2 n = I.fn32[f];
@@ -1117,8 +1107,7 @@ template <int TPF> __device__ __forceinline__ void bnd_face(const F32Inst &I, in
     double tot[4];
     group_sum<TPF, 4>(sm4, cm4, tot, S);
     if (r == 0) {
-        double g0f[4];
-        g0_fluxes(I, n64.x, n64.y, g0f);
+        const double *g0f = I.g0flux + (size_t)f * 4;
         // exact-mass wall: the g0 mass over the non-incoming set is the balance's numerator part
         tot[0] += exact_mass ? I.bnd_g0[2 * b] - rho_w * den_w : g0f[0];
         for (int q = 1; q < 4; ++q) tot[q] += g0f[q];
@@ -1174,6 +1163,18 @@ __global__ void __launch_bounds__(256) k32_bnd_setup(const F32Inst *__restrict__
             I.bnd_g0[2 * b + 1] = c;
         }
         __syncthreads();
+    }
+}
+
+// Fluxes of the reference pair along each face's n0 (static), one thread per face.
+__global__ void k32_face_setup(const F32Inst *__restrict__ insts, const int *__restrict__ foff, int ninst, int total) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int i = find_inst(foff, ninst, g);
+        const F32Inst &I = insts[i];
+        const int f = g - foff[i];
+        double o[4];
+        g0_fluxes(I, I.fn64[f].x, I.fn64[f].y, o);
+        for (int q = 0; q < 4; ++q) I.g0flux[(size_t)f * 4 + q] = o[q];
     }
 }
 
@@ -1575,6 +1576,8 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
 }
 
 int fp32_prepare(const Fp32State &s, cudaStream_t stream) {
+    k32_face_setup<<<grid_of(s.total_faces, 256, s.num_sms * 32), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
+                                                                                  s.total_faces);
     if (s.total_bnd > 0)
         k32_bnd_setup<<<grid_of(s.total_bnd, 1, s.num_sms * 32), 256, 0, stream>>>(s.d_inst, s.d_bnd_items, s.ninst,
                                                                                  s.total_bnd);

@@ -71,6 +71,7 @@ struct F32Inst {
     int vpl;                                       // velocities per lane: 1 or 2
     // physics
     double dt, hdt, R, Pr, mu0, vhs, T0, Kd, Cv, gamma, rho0;
+    float hdt32, k3_32, twoK32;  // FP32 copies of dt/2, K + 1 and 2K for the velocity loops
     // reference Maxwellian g0 (rho0, u = 0, T0) and h0 = hm0 g0: the state holds g - g0, h - h0
     double hm0;
     double gmom[10];  // sum w g0 xi^a over the velocity set: 1, x, y, xx, xy, yy, xxx, xxy, xyy, yyy
@@ -111,6 +112,7 @@ struct F32Inst {
     double *fmac;          // [F][8] rho, ux, uy, T, qx, qy, Cs, tau
     double *fgbar;         // [F][4] fluxes of the reconstructed values (mass, mom x, mom y, energy) per unit area along n0
     double *fsum;          // [F][4] same for the face equilibrium (interior) or the final boundary values
+    double *g0flux;        // [F][4] fluxes of the reference pair along n0 (static, fp32_prepare)
     float2 *bnd_in, *bnd_out;  // [nb][NVp]
     float2 *fbar;              // [F][NVp] reconstructed interior face values (moments -> update kernel)
     double *bnd_g0;            // [nb][2] half-range sums of g0 (fp32_prepare)
