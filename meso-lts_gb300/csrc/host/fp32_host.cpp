@@ -197,6 +197,7 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.fgbar = A.alloc<double>((size_t)F * 4);
         I.fsum = A.alloc<double>((size_t)F * 4);
         I.g0flux = A.alloc<double>((size_t)F * 4);
+        I.fcls = A.alloc<uint2>((size_t)F * (NVp / 32));
         I.bnd_in = A.alloc<float2>((size_t)std::max(I.nb, 1) * NVp);
         I.bnd_out = A.alloc<float2>((size_t)std::max(I.nb, 1) * NVp);
         I.bnd_g0 = A.alloc<double>(2 * (size_t)std::max(I.nb, 1));

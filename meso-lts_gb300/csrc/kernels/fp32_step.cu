@@ -64,35 +64,15 @@ __device__ __forceinline__ float fast_ex2(float x) {
     return y;
 }
 
-// True when both products of n0.xi have a zero factor in FP32 and |xi_x| + |xi_y| < 1e7 (margin
-// < 100).  The FP64 factors are then zero or below the FP32 normal range (1.2e-38), so |n0.xi| <
-// 1.2e-31 < VSMALL = 1e-30 in FP64 as well: the velocity lies between the sides (class 2) without
-// an FP64 evaluation.  This is the grazing set of axis-aligned faces (uniform meshes, walls) and
-// of velocity sets with zero components.
-__device__ __forceinline__ bool zero_products(float nx, float ny, float xx, float xy, float margin) {
-    return (nx == 0.f || xx == 0.f) && (ny == 0.f || xy == 0.f) && margin < 100.f;
+// Upwind class of velocity p at face f from the static masks (k32_cls_setup): 0 from the owner
+// (n0.xi >= VSMALL), 1 from the neighbour (< -VSMALL), 2 between (cdugks_shakhov.cpp:223-276).
+__device__ __forceinline__ int cls_bits(uint2 m, int lane) {
+    return ((m.x >> lane) & 1u) ? 0 : (((m.y >> lane) & 1u) ? 1 : 2);
 }
-
-// The same with the face's FP64 normal and the velocity's FP64 components already at hand.
-__device__ __forceinline__ int classify_r(double2 n, float2 n32, float xx, float xy, double x64, double y64, float d32,
-                                          float margin) {
-    if (d32 > margin) return 0;
-    if (d32 < -margin) return 1;
-    if (zero_products(n32.x, n32.y, xx, xy, margin)) return 2;
-    const double d = __dadd_rn(__dmul_rn(n.x, x64), __dmul_rn(n.y, y64));
-    return d >= kVSMALL ? 0 : (d < -kVSMALL ? 1 : 2);
-}
-
-// 0: from the owner (n0.xi >= VSMALL), 1: from the neighbour (< -VSMALL), 2: between.
-__device__ __forceinline__ int classify(const F32Inst &I, int f, int p, float d32, float xx, float xy) {
-    const float margin = 1e-5f * (fabsf(xx) + fabsf(xy));
-    if (d32 > margin) return 0;
-    if (d32 < -margin) return 1;
-    const float2 n32 = I.fn32[f];
-    if (zero_products(n32.x, n32.y, xx, xy, margin)) return 2;
-    const double2 n = I.fn64[f];
-    const double d = __dadd_rn(__dmul_rn(n.x, I.xi64x[p]), __dmul_rn(n.y, I.xi64y[p]));
-    return d >= kVSMALL ? 0 : (d < -kVSMALL ? 1 : 2);
+__device__ __forceinline__ int cls_of(const F32Inst &I, int f, int p) {
+    const int w = p >> 5;
+    const int ch = I.vpl == 2 ? w >> 1 : w, v = w - ch * I.vpl;
+    return cls_bits(I.fcls[((size_t)ch * I.F + f) * I.vpl + v], p & 31);
 }
 
 // exp(x) - 1 in FP32 with a small relative error near 0: the Taylor series of
@@ -242,6 +222,10 @@ __device__ __forceinline__ unsigned smem_u32(const void *p) {
 __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
+// 8 bytes from global to shared (both 8-byte aligned).
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 // Waits until at most N of the thread's commit groups are still in flight.
 template <int N> __device__ __forceinline__ void cp_async_wait() {
@@ -249,8 +233,7 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
 }
 
 struct OwnedFace {     // P1: one face owned by the tile
-    double2 n64;       // FP64 normal for the exact upwind test
-    float2 n, fdo, fdn;
+    float2 fdo, fdn;   // face centre minus owner / neighbour centre
     int bnd, face;
     unsigned short os, ns;
     int pad;
@@ -261,10 +244,13 @@ template <int VPL> struct __align__(128) TileSmem {
     float2 phi[2][F32_MAX_SLOTS * SEG];         // double-buffered chunk of the tile + halo (cp.async target)
     float4 G[F32_MAX_GSLOTS * SEG];             // gradients (g_x, g_y, h_x, h_y) of tile + 1-ring cells
     float2 ga[F32_MAX_GENT];                    // gradient stencil coefficients
+    uint2 cls[2][F32_MAX_OWNED * VPL];          // upwind masks of the owned faces for the chunk (cp.async target)
+    const uint2 *cls_src;                       // masks of chunk 0 of the tile's first owned face
+    size_t cls_stride;                          // F * VPL: from one chunk's masks to the next
     int slot_cell[F32_MAX_SLOTS];
     unsigned short gnbr[F32_MAX_GENT];
     unsigned short gptr[F32_MAX_GSLOTS + 1];
-    int nS, nG, nX, base;
+    int nS, nG, nX, ncls;
     union {
         struct {
             OwnedFace of[F32_MAX_OWNED];
@@ -327,6 +313,8 @@ __device__ __forceinline__ void load_chunk(const float2 *S, int NVp, int ch, int
         const int s = i / PER, k = i - s * PER;
         cp_async16(&sm.phi[buf][s * SEG + 2 * k], S + (size_t)sm.slot_cell[s] * NVp + (size_t)ch * SEG + 2 * k);
     }
+    const uint2 *cs = sm.cls_src + (size_t)ch * sm.cls_stride;
+    for (int i = threadIdx.x; i < sm.ncls; i += kT) cp_async8(&sm.cls[buf][i], cs + i);
     cp_async_commit();
 }
 
@@ -456,11 +444,14 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
         float2 *__restrict__ bnd_in = I.bnd_in;
         float2 *__restrict__ fbar = I.fbar;
         stage_common(I, tile, sm);
+        if (threadIdx.x == 0) {
+            sm.cls_src = I.fcls + (size_t)fs * VPL;
+            sm.cls_stride = (size_t)I.F * VPL;
+            sm.ncls = nOF * VPL;
+        }
         for (int f = threadIdx.x; f < nOF; f += kT) {
             const int g = fs + f;
             OwnedFace o;
-            o.n64 = I.fn64[g];
-            o.n = I.fn32[g];
             o.fdo = I.fdo[g];
             o.fdn = I.fdn[g];
             o.bnd = I.fbnd[g];
@@ -477,20 +468,14 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
             next_chunk<VPL>(S, NVp, ch, ch1, buf, sm);
             gradients(sm, buf, grad_on);
             __syncthreads();
-            float xx[VPL], xy[VPL], hx[VPL], hy[VPL], mg[VPL];
-            double x64[VPL], y64[VPL];
+            float hx[VPL], hy[VPL];
             int p[VPL];
 #pragma unroll
             for (int v = 0; v < VPL; ++v) {
                 p[v] = ch * SEG + v * 32 + lane;
                 const float4 t = vt32[p[v]];
-                xx[v] = t.x;
-                xy[v] = t.y;
-                x64[v] = I.xi64x[p[v]];
-                y64[v] = I.xi64y[p[v]];
-                mg[v] = 1e-5f * (fabsf(xx[v]) + fabsf(xy[v]));
-                hx[v] = hdt * xx[v];
-                hy[v] = hdt * xy[v];
+                hx[v] = hdt * t.x;
+                hy[v] = hdt * t.y;
             }
 #pragma unroll 2
             for (int fl = warp; fl < nOF; fl += F32_WARPS) {
@@ -503,8 +488,7 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
                     float2 *dst = fbar + (size_t)o.face * NVp;
 #pragma unroll
                     for (int v = 0; v < VPL; ++v) {
-                        const int cls = classify_r(o.n64, o.n, xx[v], xy[v], x64[v], y64[v],
-                                                   fmaf(o.n.x, xx[v], o.n.y * xy[v]), mg[v]);
+                        const int cls = cls_bits(sm.cls[buf][fl * VPL + v], lane);
                         dst[p[v]] = face_bar(sm, buf, v, cls, o.os, o.ns, o.fdo, o.fdn, hx[v], hy[v]);
                     }
                 }
@@ -1033,7 +1017,7 @@ template <int TPF> __device__ __forceinline__ void bnd_face(const F32Inst &I, in
             const float4 t = I.vt32[p];
             const float xx = t.x, xy = t.y, w = t.z;
             const float d = fmaf(n.x, xx, n.y * xy);
-            const int cls = classify(I, f, p, d, xx, xy);
+            const int cls = cls_of(I, f, p);
             if (cls == 1) {  // kn = -d >= VSMALL
                 const float E = fmaf(ew.ea, fmaf(xx, xx, xy * xy), fmaf(ew.ebx, xx, fmaf(ew.eby, xy, ew.ec)));
                 kahan(s2[1], c2[1], -d * w * t.w * expm1_dev(E));
@@ -1073,7 +1057,7 @@ template <int TPF> __device__ __forceinline__ void bnd_face(const F32Inst &I, in
         float2 v = bin[p];
         int cls = 0;
         if (mode != 0 && p < I.NV) {
-            cls = classify(I, f, p, d, xx, xy);
+            cls = cls_of(I, f, p);
             if (mode == 4) {
                 const float2 rv = bin[I.sym[3 * p + dir]];
                 if (cls == 1) v = rv;
@@ -1151,7 +1135,7 @@ __global__ void __launch_bounds__(256) k32_bnd_setup(const F32Inst *__restrict__
         double s0 = 0.0, s1 = 0.0;
         for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
             const float xx = I.xi32x[p], xy = I.xi32y[p];
-            const int cls = classify(I, f, p, fmaf(n.x, xx, n.y * xy), xx, xy);
+            const int cls = cls_of(I, f, p);
             const double d = n64.x * I.xi64x[p] + n64.y * I.xi64y[p];
             const double t = d * I.w64[p] * I.g0_64[p];
             if (cls == 1) s1 -= t;
@@ -1163,6 +1147,33 @@ __global__ void __launch_bounds__(256) k32_bnd_setup(const F32Inst *__restrict__
             I.bnd_g0[2 * b + 1] = c;
         }
         __syncthreads();
+    }
+}
+
+// Upwind masks of every face (static: geometry and velocity set), one warp per face: for each word
+// of 32 velocities (chunk ch, slot v of the lane layout) bit l of .x is set when velocity
+// 32 (ch VPL + v) + l upwinds from the owner (n0.xi >= VSMALL, in FP64 in the reference's order,
+// cdugks_shakhov.cpp:223-276), bit l of .y when it upwinds from the neighbour (< -VSMALL); neither
+// bit: between, the average of both sides.  Layout [chunk][face][v].
+__global__ void __launch_bounds__(256) k32_cls_setup(const F32Inst *__restrict__ insts, const int *__restrict__ foff,
+                                                    int ninst, int total) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
+        const int i = find_inst(foff, ninst, g);
+        const F32Inst &I = insts[i];
+        const int f = g - foff[i];
+        const double2 n = I.fn64[f];
+        for (int w = 0; w < I.NVp / 32; ++w) {
+            const int p = 32 * w + lane;
+            const double d = __dadd_rn(__dmul_rn(n.x, I.xi64x[p]), __dmul_rn(n.y, I.xi64y[p]));
+            const unsigned own = __ballot_sync(0xffffffffu, d >= kVSMALL);
+            const unsigned nei = __ballot_sync(0xffffffffu, d < -kVSMALL);
+            if (lane == 0) {
+                const int ch = w / I.vpl, v = w - ch * I.vpl;
+                I.fcls[((size_t)ch * I.F + f) * I.vpl + v] = make_uint2(own, nei);
+            }
+        }
     }
 }
 
@@ -1576,6 +1587,8 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
 }
 
 int fp32_prepare(const Fp32State &s, cudaStream_t stream) {
+    k32_cls_setup<<<grid_of(s.total_faces, 8, s.num_sms * 32), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
+                                                                               s.total_faces);
     k32_face_setup<<<grid_of(s.total_faces, 256, s.num_sms * 32), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
                                                                                   s.total_faces);
     if (s.total_bnd > 0)

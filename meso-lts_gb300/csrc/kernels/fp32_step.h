@@ -104,6 +104,7 @@ struct F32Inst {
     const float4 *vt32;    // [NVp] (xi_x, xi_y, w, g0) packed for one 16-byte load
     const double *g0_64;
     const int *sym;
+    uint2 *fcls;           // [chunks][F][vpl] upwind masks of each face (fp32_prepare)
     // state and work buffers
     float2 *S[2];          // [C][NVp] (g - g0, h - h0) ping-pong; S[status->step & 1] is current
     float2 *u32;           // [C] cell velocity (FP32) = reference velocity of the face moments
