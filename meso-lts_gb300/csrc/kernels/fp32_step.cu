@@ -56,6 +56,7 @@ namespace meso {
 namespace {
 
 constexpr int kT = F32_WARPS * 32;
+constexpr int kSmallFaceLanes = 8;  // lanes per face in the moments of small velocity sets
 constexpr double kLOG2E = 1.4426950408889634;
 
 __device__ __forceinline__ float fast_ex2(float x) {
@@ -177,14 +178,15 @@ template <int N> __device__ __forceinline__ void warp_sum(float (&v)[N]) {
         for (int k = 0; k < N; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
 }
 
-// Warp sum of per-lane values hi + lo (a compensated FP32 partial: hi = Kahan sum, lo = minus its
-// compensation) as an unevaluated float pair: each xor level adds the partner's pair with Knuth's
-// two-sum (exact rounding error of hi + hi') and renormalises, so the result carries about 44
-// significant bits (the pair's precision) at FP32 instruction rates.  Every lane receives the
-// same, order-independent-of-lane value; the FP64 result is hi + lo.
-__device__ __forceinline__ double warp_sum_ff(float hi, float lo) {
+// Sum over aligned groups of W lanes (W = 32: the warp) of per-lane values hi + lo (a compensated
+// FP32 partial: hi = Kahan sum, lo = minus its compensation) as an unevaluated float pair: each xor
+// level adds the partner's pair with Knuth's two-sum (exact rounding error of hi + hi') and
+// renormalises, so the result carries about 44 significant bits (the pair's precision) at FP32
+// instruction rates.  Every lane of a group receives the same, order-independent-of-lane value;
+// the FP64 result is hi + lo.  All 32 lanes of the warp must call it.
+template <int W = 32> __device__ __forceinline__ double warp_sum_ff(float hi, float lo) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = W / 2; o > 0; o >>= 1) {
         const float bh = __shfl_xor_sync(0xffffffffu, hi, o), bl = __shfl_xor_sync(0xffffffffu, lo, o);
         const float sum = __fadd_rn(hi, bh);
         const float bv = __fsub_rn(sum, hi);
@@ -645,11 +647,11 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
 // =============================================================================
 // FMa: face moments from the stored reconstructions (one warp per face), face macros in FP64
 // =============================================================================
-// Two forms, each launched over the faces of the instances of its class: large velocity sets
-// (NVp > F32_SMALL_NVP: long streaming loops, blocks of 4 velocities per lane, FP64 warp sums) and
-// small ones (blocks of 8, float-float warp sums, which cost a fraction of the FP64 pipe time
-// that dominates short faces).
-template <int NB, bool SMALL>
+// Two kernels, each launched over the faces of the instances of its class: large velocity sets
+// (NVp > F32_SMALL_NVP: a warp per face, long streaming loops, blocks of NB velocities per lane,
+// FP64 warp sums) and small ones (k32_face_moments_small: a group of L lanes per face, so the
+// cross-lane sums, which dominate short faces, are shorter and shared by 32 / L faces).
+template <int NB>
 __global__ void __launch_bounds__(256) k32_face_moments(const F32Inst *__restrict__ insts, const int *__restrict__ foff,
                                                        int ninst, int total) {
     const int lane = threadIdx.x & 31;
@@ -657,7 +659,7 @@ __global__ void __launch_bounds__(256) k32_face_moments(const F32Inst *__restric
     for (int g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
         const int i = find_inst(foff, ninst, g);
         const F32Inst &I = insts[i];
-        if (step_stopped(I.status) || (I.NVp <= F32_SMALL_NVP) != SMALL) continue;
+        if (step_stopped(I.status) || I.NVp <= F32_SMALL_NVP) continue;
         const int f = g - foff[i];
         const float2 uo = I.u32[I.fown[f]], un = I.u32[I.fnei[f]];
         const float u0xf = 0.5f * (uo.x + un.x), u0yf = 0.5f * (uo.y + un.y);
@@ -705,14 +707,10 @@ __global__ void __launch_bounds__(256) k32_face_moments(const F32Inst *__restric
         double M[F32_NMOM];
 #pragma unroll
         for (int k = 0; k < F32_NMOM; ++k) {
-            if (SMALL) {
-                M[k] = warp_sum_ff(s[k], -c[k]);
-            } else {
-                double v = (double)s[k] - (double)c[k];
+            double v = (double)s[k] - (double)c[k];
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                M[k] = v;
-            }
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            M[k] = v;
         }
         if (lane < F32_NMOM) {
             double mine = M[0];
@@ -720,6 +718,85 @@ __global__ void __launch_bounds__(256) k32_face_moments(const F32Inst *__restric
             for (int k = 1; k < F32_NMOM; ++k)
                 if (lane == k) mine = M[k];
             I.fmom[(size_t)f * F32_NMOM + lane] = mine;
+        }
+    }
+}
+
+// The moments of faces of small velocity sets: L lanes per face, 32 / L faces per warp, blocks of
+// NB velocities per lane, float-float sums over the L lanes.  Lanes of a group whose face is past
+// the end, stopped or of the other class accumulate nothing but still take part in the sums.
+template <int NB, int L>
+__global__ void __launch_bounds__(256) k32_face_moments_small(const F32Inst *__restrict__ insts,
+                                                             const int *__restrict__ foff, int ninst, int total) {
+    constexpr int FPW = 32 / L;
+    const int lane = threadIdx.x & 31, sl = lane % L;
+    const int wpb = blockDim.x >> 5;
+    for (int g0 = (blockIdx.x * wpb + (threadIdx.x >> 5)) * FPW; g0 < total; g0 += gridDim.x * wpb * FPW) {
+        const int g = g0 + lane / L;
+        int i = 0, f = 0;
+        bool on = g < total;
+        if (on) {
+            i = find_inst(foff, ninst, g);
+            on = !step_stopped(insts[i].status) && insts[i].NVp <= F32_SMALL_NVP;
+            f = g - foff[i];
+        }
+        float s[F32_NMOM], c[F32_NMOM];
+#pragma unroll
+        for (int k = 0; k < F32_NMOM; ++k) s[k] = c[k] = 0.f;
+        if (on) {
+            const F32Inst &I = insts[i];
+            const float2 uo = I.u32[I.fown[f]], un = I.u32[I.fnei[f]];
+            const float u0xf = 0.5f * (uo.x + un.x), u0yf = 0.5f * (uo.y + un.y);
+            const int b = I.fbnd[f];
+            const float2 *__restrict__ src = b >= 0 ? I.bnd_in + (size_t)b * I.NVp : I.fbar + (size_t)f * I.NVp;
+            const float4 *__restrict__ vt32 = I.vt32;
+            for (int p0 = 0; p0 < I.NVp; p0 += L * NB) {
+                float4 tv[NB];
+                float2 gv[NB];
+#pragma unroll
+                for (int j = 0; j < NB; ++j) {
+                    const int p = p0 + L * j + sl;
+                    tv[j] = p < I.NVp ? vt32[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    gv[j] = p < I.NVp ? src[p] : make_float2(0.f, 0.f);
+                }
+                float m[F32_NMOM];
+#pragma unroll
+                for (int k = 0; k < F32_NMOM; ++k) m[k] = 0.f;
+#pragma unroll
+                for (int j = 0; j < NB; ++j) {
+                    const float c0x = tv[j].x - u0xf, c0y = tv[j].y - u0yf;
+                    const float wg = tv[j].z * gv[j].x, wh = tv[j].z * gv[j].y;
+                    const float cc = fmaf(c0x, c0x, c0y * c0y);
+                    const float a = c0x * wg, bb = c0y * wg;
+                    m[0] += wg;
+                    m[1] += a;
+                    m[2] += bb;
+                    m[3] = fmaf(c0x, a, m[3]);
+                    m[4] = fmaf(c0x, bb, m[4]);
+                    m[5] = fmaf(c0y, bb, m[5]);
+                    m[6] = fmaf(cc, a, m[6]);
+                    m[7] = fmaf(cc, bb, m[7]);
+                    m[8] += wh;
+                    m[9] = fmaf(c0x, wh, m[9]);
+                    m[10] = fmaf(c0y, wh, m[10]);
+                }
+#pragma unroll
+                for (int k = 0; k < F32_NMOM; ++k) kahan(s[k], c[k], m[k]);
+            }
+        }
+        double M[F32_NMOM];
+#pragma unroll
+        for (int k = 0; k < F32_NMOM; ++k) M[k] = warp_sum_ff<L>(s[k], -c[k]);
+        if (on) {
+#pragma unroll
+            for (int k0 = 0; k0 < F32_NMOM; k0 += L) {
+                const int k = k0 + sl;
+                double mine = 0.0;
+#pragma unroll
+                for (int q = 0; q < F32_NMOM; ++q)
+                    if (q == k) mine = M[q];
+                if (k < F32_NMOM) insts[i].fmom[(size_t)f * F32_NMOM + k] = mine;
+            }
         }
     }
 }
@@ -1540,11 +1617,11 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     tiles(false);
     mark(1);
     if (s.has_large)
-        k32_face_moments<4, false><<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items,
-                                                                                   s.ninst, s.total_faces);
+        k32_face_moments<4><<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
+                                                                            s.total_faces);
     if (s.has_small)
-        k32_face_moments<8, true><<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items,
-                                                                                  s.ninst, s.total_faces);
+        k32_face_moments_small<8, kSmallFaceLanes><<<grid_of(s.total_faces, 8 * 32 / kSmallFaceLanes, cap), 256, 0,
+                                                     stream>>>(s.d_inst, s.d_face_items, s.ninst, s.total_faces);
     n += (s.has_large ? 1 : 0) + (s.has_small ? 1 : 0) - 1;
     k32_face_macros<<<grid_of(s.total_faces, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
                                                                           s.total_faces);
