@@ -864,6 +864,49 @@ __global__ void k32_face_macros(const F32Inst *__restrict__ insts, const int *__
 // =============================================================================
 // FMb: discrete moment fluxes of the face equilibrium (one warp per interior face)
 // =============================================================================
+// One block of 8 velocities per lane of one interior face (velocities p0 + L j + sl): the face's
+// flux values (n0.xi) A (blend of the reconstruction and the equilibrium, cdugks_shakhov.cpp:350-361)
+// written in place of the reconstruction for the update kernel, and the moment fluxes of the face
+// equilibrium added to the lane's compensated partials.  The block's table entries and stored
+// reconstructions are loaded before any is used.
+template <int L>
+__device__ __forceinline__ void eqflux_block(const FaceK &k, float2 n, float area, float k3, float twoK,
+                                             const float4 *__restrict__ vt32, float2 *__restrict__ fb, int NVp,
+                                             int p0, int sl, float (&s)[4], float (&c)[4]) {
+    float b[4] = {0.f, 0.f, 0.f, 0.f};
+    float4 tv[8];
+    float2 gv[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int p = p0 + L * i + sl;
+        if (p < NVp) {
+            tv[i] = vt32[p];
+            gv[i] = fb[p];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int p = p0 + L * i + sl;
+        if (p >= NVp) continue;
+        const float4 t = tv[i];
+        const float xx = t.x, xy = t.y, w = t.z;
+        const float x2 = fmaf(xx, xx, xy * xy);
+        const float2 gs = dshakhov(k.e, xx, xy, x2, t.w, k3, twoK);
+        const float2 gb = gv[i];
+        const float d = fmaf(n.x, xx, n.y * xy), knA = d * area;
+        fb[p] = make_float2(knA * fmaf(k.oCs, gb.x, k.Cs * gs.x), knA * fmaf(k.oCs, gb.y, k.Cs * gs.y));
+        const float wkn = w * d;
+        const float a = wkn * gs.x;
+        b[0] += a;
+        b[1] = fmaf(a, xx, b[1]);
+        b[2] = fmaf(a, xy, b[2]);
+        b[3] = fmaf(wkn, fmaf(x2, gs.x, gs.y), b[3]);
+    }
+    for (int q = 0; q < 4; ++q) kahan(s[q], c[q], b[q]);
+}
+
+// Large velocity sets: a warp per interior face, plain FP32 sums over blocks of 8 velocities per
+// lane, compensated across blocks, one FP32 warp sum per face.
 __global__ void __launch_bounds__(256) k32_face_eqflux(const F32Inst *__restrict__ insts, const int *__restrict__ foff,
                                                       int ninst, int total) {
     const int lane = threadIdx.x & 31;
@@ -871,57 +914,56 @@ __global__ void __launch_bounds__(256) k32_face_eqflux(const F32Inst *__restrict
     for (int g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
         const int i = find_inst(foff, ninst, g);
         const F32Inst &I = insts[i];
-        if (step_stopped(I.status)) continue;
+        if (step_stopped(I.status) || I.NVp <= F32_SMALL_NVP) continue;
         const int f = g - foff[i];
         if (I.fbnd[f] >= 0) continue;
         const FaceK k = I.fk[f];
-        const float2 n = I.fn32[f];
-        const float area = I.farea[f];
-        const float k3 = I.k3_32, twoK = I.twoK32;
-        const float4 *__restrict__ vt32 = I.vt32;
-        float2 *__restrict__ fb = I.fbar + (size_t)f * I.NVp;
-        // plain FP32 sums over blocks of 8 velocities per lane, compensated across blocks; each
-        // block's table entries and stored reconstructions are loaded before any is used
         float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int p0 = 0; p0 < I.NVp; p0 += 32 * 8) {
-            float b[4] = {0.f, 0.f, 0.f, 0.f};
-            float4 tv[8];
-            float2 gv[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int p = p0 + 32 * i + lane;
-                if (p < I.NVp) {
-                    tv[i] = vt32[p];
-                    gv[i] = fb[p];
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int p = p0 + 32 * i + lane;
-                if (p >= I.NVp) continue;
-                const float4 t = tv[i];
-                const float xx = t.x, xy = t.y, w = t.z;
-                const float x2 = fmaf(xx, xx, xy * xy);
-                const float2 gs = dshakhov(k.e, xx, xy, x2, t.w, k3, twoK);
-                // the face's flux value (n0.xi) A (blend of the reconstruction and the equilibrium,
-                // cdugks_shakhov.cpp:350-361), in place of the reconstruction, for the update kernel
-                const float2 gb = gv[i];
-                const float d = fmaf(n.x, xx, n.y * xy), knA = d * area;
-                fb[p] = make_float2(knA * fmaf(k.oCs, gb.x, k.Cs * gs.x), knA * fmaf(k.oCs, gb.y, k.Cs * gs.y));
-                const float wkn = w * d;
-                const float a = wkn * gs.x;
-                b[0] += a;
-                b[1] = fmaf(a, xx, b[1]);
-                b[2] = fmaf(a, xy, b[2]);
-                b[3] = fmaf(wkn, fmaf(x2, gs.x, gs.y), b[3]);
-            }
-            for (int q = 0; q < 4; ++q) kahan(s[q], c[q], b[q]);
-        }
+        float2 *__restrict__ fb = I.fbar + (size_t)f * I.NVp;
+        for (int p0 = 0; p0 < I.NVp; p0 += 32 * 8)
+            eqflux_block<32>(k, I.fn32[f], I.farea[f], I.k3_32, I.twoK32, I.vt32, fb, I.NVp, p0, lane, s, c);
         float v[4] = {s[0] - c[0], s[1] - c[1], s[2] - c[2], s[3] - c[3]};
         warp_sum(v);
         if (lane < 4) {
             const double *g0f = I.g0flux + (size_t)f * 4;
             I.fsum[(size_t)f * 4 + lane] = g0f[lane] + (double)pick(v, lane);
+        }
+    }
+}
+
+// Small velocity sets: L lanes per interior face, 32 / L faces per warp, sums over the L lanes.
+// Lanes of a group without a face to do accumulate nothing but take part in the sums.
+template <int L>
+__global__ void __launch_bounds__(256) k32_face_eqflux_small(const F32Inst *__restrict__ insts,
+                                                            const int *__restrict__ foff, int ninst, int total) {
+    constexpr int FPW = 32 / L;
+    const int lane = threadIdx.x & 31, sl = lane % L;
+    const int wpb = blockDim.x >> 5;
+    for (int g0 = (blockIdx.x * wpb + (threadIdx.x >> 5)) * FPW; g0 < total; g0 += gridDim.x * wpb * FPW) {
+        const int g = g0 + lane / L;
+        int i = 0, f = 0;
+        bool on = g < total;
+        if (on) {
+            i = find_inst(foff, ninst, g);
+            f = g - foff[i];
+            on = !step_stopped(insts[i].status) && insts[i].NVp <= F32_SMALL_NVP && insts[i].fbnd[f] < 0;
+        }
+        float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
+        if (on) {
+            const F32Inst &I = insts[i];
+            const FaceK k = I.fk[f];
+            float2 *__restrict__ fb = I.fbar + (size_t)f * I.NVp;
+            for (int p0 = 0; p0 < I.NVp; p0 += L * 8)
+                eqflux_block<L>(k, I.fn32[f], I.farea[f], I.k3_32, I.twoK32, I.vt32, fb, I.NVp, p0, sl, s, c);
+        }
+        float v[4] = {s[0] - c[0], s[1] - c[1], s[2] - c[2], s[3] - c[3]};
+#pragma unroll
+        for (int o = L / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+        if (on && sl < 4) {
+            const double *g0f = insts[i].g0flux + (size_t)f * 4;
+            insts[i].fsum[(size_t)f * 4 + sl] = g0f[sl] + (double)pick(v, sl);
         }
     }
 }
@@ -1634,8 +1676,13 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
                                                                                      s.nbnd_blocks);
         cudaEventRecord(fork->join, fork->side);
     }
-    k32_face_eqflux<<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
-                                                                        s.total_faces);
+    if (s.has_large)
+        k32_face_eqflux<<<grid_of(s.total_faces, 8, cap), 256, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
+                                                                            s.total_faces);
+    if (s.has_small)
+        k32_face_eqflux_small<kSmallFaceLanes><<<grid_of(s.total_faces, 8 * 32 / kSmallFaceLanes, cap), 256, 0,
+                                                 stream>>>(s.d_inst, s.d_face_items, s.ninst, s.total_faces);
+    n += (s.has_large ? 1 : 0) + (s.has_small ? 1 : 0) - 1;
     mark(3);
     n += 3;
     if (branch) {
