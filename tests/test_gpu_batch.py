@@ -17,6 +17,8 @@ MEMBERS = [
     ("jquad_nc21", lambda d: cases.shakhov_cavity(d, "jquad", 14, "nc", 21, 1.0, 0.1, 50, seed=3)),
     ("quad_d2q9", lambda d: cases.shakhov_cavity(d, "quad", 12, "d2q9", 3, 0.05, 0.12, 50)),
     ("channel_pressure", lambda d: cases.shakhov_channel(d, "pressure", 12, 6, "hgh", 8, 0.2, 50)),
+    # a large velocity set (NC 51^2): the batch launches the large- and small-set face kernels
+    ("jquad_nc51", lambda d: cases.shakhov_cavity(d, "jquad", 8, "nc", 51, 1.0, 0.15, 50, seed=4)),
 ]
 
 

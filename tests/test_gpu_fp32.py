@@ -22,6 +22,8 @@ CASES = [
     ("jquad_nc21_kn1", lambda d: cases.shakhov_cavity(d, "jquad", 12, "nc", 21, 1.0, 0.15, 60), 60),
     ("quad_d2q9_kn0.05", lambda d: cases.shakhov_cavity(d, "quad", 10, "d2q9", 3, 0.05, 0.15, 60), 60),
     ("quad_hgh28_kn0.075", lambda d: cases.shakhov_cavity(d, "quad", 12, "hgh", 28, 0.075, 0.15, 40), 40),
+    # NC 51^2 = 2601 velocities: the large-set kernels (warp-per-face sums, a block per boundary face)
+    ("jquad_nc51_kn1", lambda d: cases.shakhov_cavity(d, "jquad", 8, "nc", 51, 1.0, 0.15, 40, seed=4), 40),
     ("quad_nograd", lambda d: cases.shakhov_cavity(d, "quad", 10, "hgh", 8, 0.1, 0.15, 40, gradient=False), 40),
     ("channel_pressure", lambda d: cases.shakhov_channel(d, "pressure", 12, 6, "hgh", 8, 0.2, 40), 40),
     ("channel_farfield", lambda d: cases.shakhov_channel(d, "farfield", steps=40), 40),
