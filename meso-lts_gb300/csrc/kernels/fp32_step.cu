@@ -320,17 +320,14 @@ __device__ __forceinline__ void load_chunk(const float2 *S, int NVp, int ch, int
     cp_async_commit();
 }
 
-// Makes chunk `ch` (issued one iteration earlier) visible to the CTA and starts the copies of chunk
-// ch + 1 into the other buffer, which the previous iteration has finished reading.
+// Makes chunk `ch` (issued one iteration earlier) visible to the CTA; the barrier also certifies
+// that every warp has finished the previous iteration, which read the other buffer and the
+// gradients, so the copies of chunk ch + 1 go into that buffer right after it.
 template <int VPL>
 __device__ __forceinline__ void next_chunk(const float2 *S, int NVp, int ch, int ch1, int buf, TileSmem<VPL> &sm) {
-    if (ch + 1 < ch1) {
-        load_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
-        cp_async_wait<1>();
-    } else {
-        cp_async_wait<0>();
-    }
+    cp_async_wait<0>();
     __syncthreads();
+    if (ch + 1 < ch1) load_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
 }
 
 // Gradients of the first nG slots from phi[buf].
@@ -495,8 +492,8 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
                     }
                 }
             }
-            __syncthreads();
         }
+        __syncthreads();  // the next item restages the tile tables
     }
 }
 
@@ -565,13 +562,10 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         load_upd_chunk<VPL>(S, NVp, ch0, 0, sm);
         for (int ch = ch0; ch < ch1; ++ch) {
             const int buf = (ch - ch0) & 1;
-            if (ch + 1 < ch1) {
-                load_upd_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
-                cp_async_wait<1>();
-            } else {
-                cp_async_wait<0>();
-            }
+            // chunk ch visible; every warp has finished chunk ch - 1, so its buffer takes chunk ch + 1
+            cp_async_wait<0>();
             __syncthreads();
+            if (ch + 1 < ch1) load_upd_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
             float xx[VPL], xy[VPL], w[VPL], g0[VPL], x2[VPL];
             int p[VPL];
 #pragma unroll
@@ -628,7 +622,6 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
                 kahan(qs[r][0], qc[r][0], qv[0]);
                 kahan(qs[r][1], qc[r][1], qv[1]);
             }
-            __syncthreads();
         }
 #pragma unroll
         for (int r = 0; r < RC; ++r) {  // one float-float warp reduction per cell and item
