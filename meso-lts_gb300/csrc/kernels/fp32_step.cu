@@ -55,7 +55,11 @@
 namespace meso {
 namespace {
 
-constexpr int kT = F32_WARPS * 32;
+constexpr int kRW = 24;       // warps of the reconstruction kernel
+constexpr int kT = kRW * 32;
+// Both tile kernels run 24 warps in their one CTA per SM (the register budget is then 85 per
+// thread); the update kernel's warps take two cells of a 48-cell tile each.
+constexpr int kUW = 24, kUT = kUW * 32;
 constexpr int kSmallFaceLanes = 8;  // lanes per face in the moments of small velocity sets
 constexpr double kLOG2E = 1.4426950408889634;
 
@@ -336,7 +340,7 @@ template <int VPL> __device__ __forceinline__ void gradients(TileSmem<VPL> &sm, 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nG = sm.nG;
     const float2 *phi = sm.phi[buf];
-    for (int s = warp; s < nG; s += F32_WARPS) {
+    for (int s = warp; s < nG; s += kRW) {
         float4 g[VPL];
         float2 c[VPL];
 #pragma unroll
@@ -477,7 +481,7 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
                 hy[v] = hdt * t.y;
             }
 #pragma unroll 2
-            for (int fl = warp; fl < nOF; fl += F32_WARPS) {
+            for (int fl = warp; fl < nOF; fl += kRW) {
                 const OwnedFace o = sm.u.p1.of[fl];
                 if (o.bnd >= 0) {  // own = neighbour: every upwind choice gives the owner's reconstruction
                     float2 *dst = bnd_in + (size_t)o.bnd * NVp;
@@ -506,7 +510,7 @@ template <int VPL>
 __device__ __forceinline__ void load_upd_chunk(const float2 *S, int NVp, int ch, int buf, UpdSmem<VPL> &sm) {
     constexpr int SEG = UpdSmem<VPL>::SEG, PER = SEG / 2;
     const int nc = sm.nc, ntf = sm.ntf;
-    for (int i = threadIdx.x; i < (nc + ntf) * PER; i += kT) {
+    for (int i = threadIdx.x; i < (nc + ntf) * PER; i += kUT) {
         const int s = i / PER, k = i - s * PER;
         if (s < nc)
             cp_async16(&sm.phi[buf][s * SEG + 2 * k], S + (size_t)(sm.cs + s) * NVp + (size_t)ch * SEG + 2 * k);
@@ -517,7 +521,7 @@ __device__ __forceinline__ void load_upd_chunk(const float2 *S, int NVp, int ch,
 }
 
 template <int VPL>
-__global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
+__global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
                                                    int nitems) {
     constexpr int SEG = UpdSmem<VPL>::SEG;
     extern __shared__ float4 smem_raw[];
@@ -539,12 +543,12 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         const float k3 = I.k3_32, twoK = I.twoK32;
         const float4 *__restrict__ vt32 = I.vt32;
         const int j0 = I.cf_ptr[cs];
-        for (int c = threadIdx.x; c < nc; c += kT) sm.ck[c] = I.ck[cs + c];
-        for (int c = threadIdx.x; c <= nc; c += kT) sm.cf_off[c] = I.cf_ptr[cs + c] - j0;
+        for (int c = threadIdx.x; c < nc; c += kUT) sm.ck[c] = I.ck[cs + c];
+        for (int c = threadIdx.x; c <= nc; c += kUT) sm.cf_off[c] = I.cf_ptr[cs + c] - j0;
         const int ncf = I.cf_ptr[cs + nc] - j0;
-        for (int e = threadIdx.x; e < ncf; e += kT) sm.cft[e] = I.cf_tf[j0 + e];
+        for (int e = threadIdx.x; e < ncf; e += kUT) sm.cft[e] = I.cf_tf[j0 + e];
         const int q0 = I.tile_tf_ptr[tile], ntf = I.tile_tf_ptr[tile + 1] - q0;
-        for (int q = threadIdx.x; q < ntf; q += kT) {
+        for (int q = threadIdx.x; q < ntf; q += kUT) {
             const int f = I.tf_face[q0 + q], b = I.fbnd[f];
             sm.src[q] = b >= 0 ? I.bnd_out + (size_t)b * NVp : I.fbar + (size_t)f * NVp;
         }
@@ -555,7 +559,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         }
         __syncthreads();
         // heat-flux partials of this warp's cells (cl = warp + 16 r): per lane, compensated, across chunks
-        constexpr int RC = (F32_MAX_CELLS + F32_WARPS - 1) / F32_WARPS;
+        constexpr int RC = (F32_MAX_CELLS + kUW - 1) / kUW;
         float qs[RC][2], qc[RC][2];
 #pragma unroll
         for (int r = 0; r < RC; ++r) qs[r][0] = qs[r][1] = qc[r][0] = qc[r][1] = 0.f;
@@ -580,7 +584,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
             }
 #pragma unroll
             for (int r = 0; r < RC; ++r) {
-                const int cl = warp + F32_WARPS * r;
+                const int cl = warp + kUW * r;
                 if (cl >= nc) break;
                 float fg[VPL], fh[VPL];
 #pragma unroll
@@ -625,7 +629,7 @@ __global__ void __launch_bounds__(kT, 1) k32_update(const F32Inst *__restrict__ 
         }
 #pragma unroll
         for (int r = 0; r < RC; ++r) {  // one float-float warp reduction per cell and item
-            const int cl = warp + F32_WARPS * r;
+            const int cl = warp + kUW * r;
             if (cl >= nc) break;
             const double q0 = warp_sum_ff(qs[r][0], -qc[r][0]), q1 = warp_sum_ff(qs[r][1], -qc[r][1]);
             if (lane == 0) {
@@ -1635,12 +1639,12 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     int n = 0;
     auto tiles = [&](bool update) {
         if (n2 > 0) {
-            if (update) k32_update<2><<<grid2, kT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
+            if (update) k32_update<2><<<grid2, kUT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
             else k32_reconstruct<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
             ++n;
         }
         if (n1 > 0) {
-            if (update) k32_update<1><<<grid1, kT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
+            if (update) k32_update<1><<<grid1, kUT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
             else k32_reconstruct<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
             ++n;
         }

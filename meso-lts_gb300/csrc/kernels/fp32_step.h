@@ -14,7 +14,6 @@
 namespace meso {
 
 // Kernel limits (the tile planner shrinks tiles until every tile fits).
-constexpr int F32_WARPS = 16;       // warps per CTA of the tile kernels
 constexpr int F32_MAX_VPL = 2;      // velocities per lane (a chunk is 32 x VPL velocities)
 constexpr int F32_MAX_SLOTS = 104;  // tile + 1-ring + (part of the) 2-ring halo cells
 constexpr int F32_MAX_GSLOTS = 72;  // slots with a gradient (tile + 1-ring cells owned faces reconstruct from)
