@@ -2,7 +2,7 @@
 //
 // The FP32 tile kernels have three shape parameters: cells per tile (which
 // sets the halo overhead, the shared-memory footprint and how evenly a tile's
-// cells split over the 16 warps), velocities per lane (1 or 2: registers and
+// cells split over the 24 warps), velocities per lane (1 or 2: registers and
 // shared memory against per-chunk overhead) and velocity groups per tile (how
 // many CTAs share one tile's velocity range).  The best choice depends on the
 // mesh and the velocity set, so it is measured: each candidate shape builds a

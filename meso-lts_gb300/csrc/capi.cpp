@@ -159,6 +159,7 @@ int build_device(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d) {
     CUDA_TRY(cudaEventCreate(&c->ev1));
     CUDA_TRY(cudaMallocHost(&c->h_status, sizeof(meso::DStatus)));
     const int C = m->ncell, F = m->nface, NV = d->nv, D = m->dim;
+    CUDA_TRY(cudaMallocHost(&c->h_mac, sizeof(double) * 8 * (size_t)C));
     const auto &rn = c->rn;
     // ---- renumbered host tables
     std::vector<double> vol(C), cpos(3 * C), lsq_c(9 * C), lsq_w, lsq_dr, farea(F), fpos(3 * F), fn(3 * F);
@@ -295,10 +296,10 @@ int build_device(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d) {
         s.flux1 = shakhov ? A.alloc<double>(cv) : nullptr;
         s.snap0 = A.alloc<double>(bv);
         s.snap1 = shakhov ? A.alloc<double>(bv) : nullptr;
-        s.rho = A.alloc<double>(C);
-        s.u = A.alloc<double>(3 * C);
-        s.T = A.alloc<double>(C);
-        s.q = A.alloc<double>(3 * C);
+        s.rho = A.alloc<double>(8 * (size_t)C);  // rho, u, T, q contiguous: one copy to the host
+        s.u = s.rho + C;
+        s.T = s.rho + 4 * (size_t)C;
+        s.q = s.rho + 5 * (size_t)C;
         s.fm0 = A.alloc<double>(C);
         s.fm1 = A.alloc<double>(3 * C);
         s.fm2 = A.alloc<double>(C);
@@ -335,24 +336,41 @@ int read_status(meso_ctx *c) {
     return MESO_OK;
 }
 
+// The macros in original cell order into the given host arrays (any may be null): one copy of the
+// contiguous device block into pinned staging, then the permutation.
+int fetch_macros(meso_ctx *c, double *rho, double *u, double *T, double *q) {
+    const size_t C = (size_t)c->C;
+    double *h = c->h_mac;
+    if (c->ps.u == c->ps.rho + C && c->ps.T == c->ps.rho + 4 * C && c->ps.q == c->ps.rho + 5 * C) {
+        CUDA_TRY(cudaMemcpyAsync(h, c->ps.rho, sizeof(double) * 8 * C, cudaMemcpyDeviceToHost, c->stream));
+    } else {
+        CUDA_TRY(cudaMemcpyAsync(h, c->ps.rho, sizeof(double) * C, cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(h + C, c->ps.u, sizeof(double) * 3 * C, cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(h + 4 * C, c->ps.T, sizeof(double) * C, cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(h + 5 * C, c->ps.q, sizeof(double) * 3 * C, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const int *n2o = c->rn.cell_new2old.data();
+    for (size_t i = 0; i < C; ++i) {
+        const size_t o = (size_t)n2o[i];
+        if (rho) rho[o] = h[i];
+        if (T) T[o] = h[4 * C + i];
+        for (int k = 0; k < 3; ++k) {
+            if (u) u[3 * o + k] = h[C + 3 * i + k];
+            if (q) q[3 * o + k] = h[5 * C + 3 * i + k];
+        }
+    }
+    return MESO_OK;
+}
+
 int download_macros(meso_ctx *c, std::vector<double> &rho, std::vector<double> &u, std::vector<double> &T,
                     std::vector<double> &q) {
-    const int C = c->C;
-    std::vector<double> r(C), uu(3 * C), t(C), qq(3 * C);
-    CUDA_TRY(cudaMemcpyAsync(r.data(), c->ps.rho, sizeof(double) * C, cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(cudaMemcpyAsync(uu.data(), c->ps.u, sizeof(double) * 3 * C, cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(cudaMemcpyAsync(t.data(), c->ps.T, sizeof(double) * C, cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(cudaMemcpyAsync(qq.data(), c->ps.q, sizeof(double) * 3 * C, cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const size_t C = (size_t)c->C;
     rho.resize(C);
     u.resize(3 * C);
     T.resize(C);
     q.resize(3 * C);
-    to_orig(c, r, rho.data(), 1);
-    to_orig(c, uu, u.data(), 3);
-    to_orig(c, t, T.data(), 1);
-    to_orig(c, qq, q.data(), 3);
-    return MESO_OK;
+    return fetch_macros(c, rho.data(), u.data(), T.data(), q.data());
 }
 
 // Solver::residual (field.cpp:223-249): sum |(new-old)/old| V/V_total in cell order; old <- new.
@@ -846,6 +864,7 @@ void meso_ctx_destroy(meso_ctx *c) {
     free_fp32_launch(c->fs, c->fs_owned);
     c->arena.release();
     if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->h_mac) cudaFreeHost(c->h_mac);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -929,7 +948,10 @@ int meso_step(meso_ctx *c, int32_t nsteps, int32_t *steps_done) {
     const int done = c->h_status->step - start;
     for (int i = 0; i < done && i < (int)dts.size(); ++i) c->solution_time += dts[i];
     c->step = c->h_status->step;
-    if (c->params.precision == MESO_FP32 && (rc = meso_host::ctx_read_resid(c))) return rc;
+    const int ri = c->params.residual_interval;
+    if (c->params.precision == MESO_FP32 && ri > 0 && c->step / ri > start / ri &&
+        (rc = meso_host::ctx_read_resid(c)))
+        return rc;
     if (steps_done) *steps_done = done;
     if (stopped || c->h_status->stop_step != INT_MAX) {
         c->run_state = 0;
@@ -941,14 +963,7 @@ int meso_step(meso_ctx *c, int32_t nsteps, int32_t *steps_done) {
 
 int meso_get_macros(meso_ctx *c, double *rho, double *u, double *T, double *q) {
     CTX_CHECK(c);
-    std::vector<double> r, uu, t, qq;
-    int rc = download_macros(c, r, uu, t, qq);
-    if (rc) return rc;
-    if (rho) std::copy(r.begin(), r.end(), rho);
-    if (u) std::copy(uu.begin(), uu.end(), u);
-    if (T) std::copy(t.begin(), t.end(), T);
-    if (q) std::copy(qq.begin(), qq.end(), q);
-    return MESO_OK;
+    return fetch_macros(c, rho, u, T, q);
 }
 
 int meso_get_flux_moments(meso_ctx *c, double *m0, double *m1, double *m2) {

@@ -67,6 +67,7 @@ struct meso_ctx {
     meso::DMesh dm{};
     meso::DStatus *d_status = nullptr;
     meso::DStatus *h_status = nullptr;  // pinned mirror
+    double *h_mac = nullptr;            // pinned staging of the macros: rho, u (3), T, q (3) per cell
     meso::PlainState ps{};
     meso::F32Inst f32{};               // FP32 instance (device pointers), when precision == MESO_FP32
     meso::Fp32State fs{};              // its single-instance launch state

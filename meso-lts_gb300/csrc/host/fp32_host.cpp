@@ -204,10 +204,10 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.fbar = A.alloc<float2>((size_t)F * NVp);
         I.ck = A.alloc<meso::CellK>(C);
         I.qpart = A.alloc<double>((size_t)I.ngroup * C * 2);
-        I.rho = A.alloc<double>(C);
-        I.u = A.alloc<double>(3 * (size_t)C);
-        I.T = A.alloc<double>(C);
-        I.q = A.alloc<double>(3 * (size_t)C);
+        I.rho = A.alloc<double>(8 * (size_t)C);  // rho, u, T, q contiguous: one copy to the host
+        I.u = I.rho + C;
+        I.T = I.rho + 4 * (size_t)C;
+        I.q = I.rho + 5 * (size_t)C;
         I.fm0 = A.alloc<double>(C);
         I.fm1 = A.alloc<double>(3 * (size_t)C);
         I.fm2 = A.alloc<double>(C);
