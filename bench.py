@@ -363,7 +363,8 @@ def run_batched(tmp: str, steps: int = 20, warm: int = 3, autotune: bool = True)
             "tuned_shapes": {f"{k[0]}^2 {k[1]}": v for k, v in tuned.items()}}
 
 
-def run_served(tmp: str, count: int = 200, rate: float = 20.0, max_step: int = 8000, poll_steps: int = 100) -> dict:
+def run_served(tmp: str, count: int = 200, rate: float = 20.0, max_step: int = 8000, poll_steps: int = 100,
+               members: int = 64) -> dict:
     """Config 5: a seeded Poisson stream of cavity solves, each run to convergence on U, served with
     continuous batching; time-to-converged per request (submit to retirement)."""
     import cases
@@ -382,7 +383,7 @@ def run_served(tmp: str, count: int = 200, rate: float = 20.0, max_step: int = 8
     rt = _cudart()
     free_b, total_b = ctypes.c_size_t(), ctypes.c_size_t()
     rt.cudaMemGetInfo(ctypes.byref(free_b), ctypes.byref(total_b))
-    srv = mg.Server(hbm_budget_bytes=int(free_b.value * 0.8), max_members=64)
+    srv = mg.Server(hbm_budget_bytes=int(free_b.value * 0.8), max_members=members)
     done = {}
     i = 0
     t0 = time.perf_counter()
@@ -423,7 +424,7 @@ def run_served(tmp: str, count: int = 200, rate: float = 20.0, max_step: int = 8
     return {"workload": f"{count} cavity solves, Poisson arrivals {rate}/s (seed 2), sides {{16,24,32}} quads, "
                         "log10 Kn ~ U(-2,0), DVS {hGH 28x28, NC 21x21}, lid ~ U(0.05,0.15), FP32 storage, "
                         f"run to L2-relative residual 1e-6 on U per 100 steps (max-step {max_step})",
-            "solves_per_s": count / wall, "wall_seconds": wall, "p50_s": q(0.50), "p99_s": q(0.99),
+            "max_members": members, "solves_per_s": count / wall, "wall_seconds": wall, "p50_s": q(0.50), "p99_s": q(0.99),
             "converged": conv, "reached_max_step_or_failed": count - conv, "mean_steps": float(np.mean(steps)),
             "serial_fp64_solves_per_s_est": count / serial_s if serial_s > 0 else None,
             "serial_fp64_note": "FP64 step time of each request class x the steps each solve took, summed"}
@@ -439,6 +440,7 @@ def main() -> int:
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--served-count", type=int, default=200)
+    ap.add_argument("--served-members", type=int, default=64, help="solves stepped together at most")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -557,7 +559,7 @@ def main() -> int:
             line["other_configs"] = run_other_configs(tmp)
             line["batched"] = run_batched(tmp)
         if not args.no_served:
-            line["served"] = run_served(tmp, count=args.served_count)
+            line["served"] = run_served(tmp, count=args.served_count, members=args.served_members)
         if rank == 0:
             print(json.dumps(line), flush=True)
     dist.close()

@@ -59,6 +59,10 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
     I.vpl = vpl;
     I.chunks = NVp / (32 * vpl);
     I.ngroup = ngroup > 0 ? std::min(ngroup, I.chunks) : default_ngroup(P.ntile, I.chunks, c->num_sms);
+    {  // groups take ceil(chunks / ngroup) chunks each: drop groups that would be left empty
+        const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
+        I.ngroup = (I.chunks + cpg - 1) / cpg;
+    }
     const meso_params &p = c->params;
     I.dt = p.dt;
     I.hdt = p.dt * 0.5;

@@ -536,7 +536,10 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
         const int cs = I.tile_cstart[tile], nc = I.tile_ncell[tile];
         const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
         const int ch0 = grp * cpg, ch1 = min(I.chunks, ch0 + cpg);
-        if (ch0 >= ch1) continue;
+        if (ch0 >= ch1) {  // an empty velocity group (not planned, see build_fp32_instance) adds nothing
+            for (int c = threadIdx.x; c < 2 * nc; c += kUT) I.qpart[((size_t)grp * I.C + cs) * 2 + c] = 0.0;
+            continue;
+        }
         const float2 *__restrict__ S = I.S[cur];
         float2 *__restrict__ Sn = I.S[cur ^ 1];
         const int NVp = I.NVp;
