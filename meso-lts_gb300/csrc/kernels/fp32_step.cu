@@ -1422,11 +1422,12 @@ __global__ void k32_heat_flux(const F32Inst *__restrict__ insts, const int *__re
 
 // cell_value_interp (cdugks_shakhov.cpp:766-789) for queued masked cells, writing state n+1
 __global__ void k32_mask_repair(const F32Inst *__restrict__ insts, int ninst) {
-    for (int i = 0; i < ninst; ++i) {
+    for (int i = blockIdx.x; i < ninst; i += gridDim.x) {  // a block per instance: repairs are rare
         const F32Inst &I = insts[i];
-        const int nxt = (I.status->step & 1) ^ 1;  // before k32_end_step advances the step
         const int n = min(I.status->repair_count, I.C);
-        for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        if (n == 0) continue;
+        const int nxt = (I.status->step & 1) ^ 1;  // before k32_end_step advances the step
+        for (int r = 0; r < n; ++r) {
             const int c = I.repair_list[r];
             double sw = 0.0, sr = 0.0, sT = 0.0, sux = 0.0, suy = 0.0, sqx = 0.0, sqy = 0.0;
             for (int j = I.cn_ptr[c]; j < I.cn_ptr[c + 1]; ++j) {
@@ -1460,6 +1461,7 @@ __global__ void k32_mask_repair(const F32Inst *__restrict__ insts, int ninst) {
                 I.u[3 * c + 1] = uy;
                 I.u32[c] = make_float2((float)ux, (float)uy);
             }
+            __syncthreads();  // the next repair's neighbour sums see this one, in every thread alike
         }
     }
 }
@@ -1701,7 +1703,7 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     mark(6);
     k32_heat_flux<<<grid_of(s.total_cells, 256, cap), 256, 0, stream>>>(s.d_inst, s.d_cell_items, s.ninst,
                                                                         s.total_cells, 1);
-    k32_mask_repair<<<32, 256, 0, stream>>>(s.d_inst, s.ninst);
+    k32_mask_repair<<<s.ninst < s.num_sms ? s.ninst : s.num_sms, 256, 0, stream>>>(s.d_inst, s.ninst);
     k32_end_step<<<(s.ninst + 63) / 64, 64, 0, stream>>>(s.d_inst, s.ninst);
     k32_residual<<<s.ninst < s.num_sms ? s.ninst : s.num_sms, 512, 0, stream>>>(s.d_inst, s.ninst);
     mark(7);
