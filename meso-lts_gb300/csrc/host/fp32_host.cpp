@@ -78,6 +78,11 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
     I.Cv = (p.K + 3.0) * p.R * 0.5;
     I.gamma = (p.K + 5.0) / (p.K + 3.0);
     I.rho0 = p.rho0 > 0.0 ? p.rho0 : 1.0;
+    I.iR = 1.0 / I.R;
+    I.iT0 = 1.0 / I.T0;
+    I.iCv = 1.0 / I.Cv;
+    I.iRT0 = 1.0 / (I.R * I.T0);
+    I.irho0 = 1.0 / I.rho0;
     I.hm0 = (p.K + 1.0) * p.R * p.T0;
     I.gradient = p.gradient_switch;
     I.res_interval = p.residual_interval;

@@ -115,25 +115,42 @@ __device__ __forceinline__ float2 dshakhov(const EqP &e, float xx, float xy, flo
     return make_float2(dg, dh);
 }
 
-// EqP of (rho, u, T, q), from FP64 macros.
-__device__ __forceinline__ EqP make_eqp(const F32Inst &I, double rho, double ux, double uy, double T, double qx,
-                                        double qy) {
-    const double RT = I.R * T, p = rho * RT, iRT = 1.0 / RT;
+// EqP of (rho, u, T, q), from FP64 macros, given irho = 1 / rho and iRT = 1 / (R T): FP64 runs at
+// a small fraction of the FP32 rate here, so the per-face and per-cell scalar work shares its
+// reciprocals instead of dividing again.
+__device__ __forceinline__ EqP make_eqp_r(const F32Inst &I, double rho, double irho, double ux, double uy, double T,
+                                          double iRT, double qx, double qy) {
+    const double RT = I.R * T, ip = irho * iRT, c1 = (1.0 - I.Pr) * 0.2;
     EqP e;
     e.ux = (float)ux;
     e.uy = (float)uy;
     e.qx = (float)qx;
     e.qy = (float)qy;
-    e.ea = (float)(0.5 / (I.R * I.T0) - 0.5 * iRT);
+    e.ea = (float)(0.5 * (I.iRT0 - iRT));
     e.ebx = (float)(ux * iRT);
     e.eby = (float)(uy * iRT);
-    e.ec = (float)(log(rho * I.T0 / (I.rho0 * T)) - 0.5 * (ux * ux + uy * uy) * iRT);
-    e.sg = (float)((1.0 - I.Pr) / (5.0 * p * RT));
-    e.sh = (float)((1.0 - I.Pr) / (5.0 * p));
+    e.ec = (float)(log(rho * I.irho0 * (I.T0 * I.R * iRT)) - 0.5 * (ux * ux + uy * uy) * iRT);
+    e.sg = (float)(c1 * ip * iRT);  // (1 - Pr) / (5 p R T)
+    e.sh = (float)(c1 * ip);        // (1 - Pr) / (5 p)
     e.iRT = (float)iRT;
     e.hm = (float)((I.Kd + 1.0) * RT);
     e.dhm = (float)((I.Kd + 1.0) * I.R * (T - I.T0));
     return e;
+}
+
+__device__ __forceinline__ EqP make_eqp(const F32Inst &I, double rho, double ux, double uy, double T, double qx,
+                                        double qy) {
+    return make_eqp_r(I, rho, 1.0 / rho, ux, uy, T, 1.0 / (I.R * T), qx, qy);
+}
+
+// (T / T0)^omega: the square root for the common omega = 1/2.
+__device__ __forceinline__ double vhs_pow(const F32Inst &I, double t_ratio) {
+    return I.vhs == 0.5 ? sqrt(t_ratio) : pow(t_ratio, I.vhs);
+}
+
+// tau = mu0 (T / T0)^omega / (rho R T) (cdugks_shakhov.cpp:181-183) from the reciprocals of rho and T.
+__device__ __forceinline__ double tau_r(const F32Inst &I, double irho, double T, double iT) {
+    return I.mu0 * vhs_pow(I, T * I.iT0) * irho * iT * I.iR;
 }
 
 // The 11 raw moments of the reference pair about velocity (a, b), from the discrete
@@ -818,14 +835,14 @@ __global__ void k32_face_macros(const F32Inst *__restrict__ insts, const int *__
             g0_raw_moments(I, u0x, u0y, M0);
             for (int k = 0; k < F32_NMOM; ++k) M[k] += M0[k];
         }
-        const double rho = M[0];
-        const double dx = M[1] / rho, dy = M[2] / rho;
+        const double rho = M[0], irho = 1.0 / rho;
+        const double dx = M[1] * irho, dy = M[2] * irho;
         const double ux = u0x + dx, uy = u0y + dy;
         const double trM = M[3] + M[5];
         const double dd = dx * dx + dy * dy;
         const double e2 = trM - rho * dd + M[8];  // sum w (|xi-u|^2 g + h)
-        const double T = (0.5 * e2 / rho) / I.Cv;
-        const double tau = I.mu0 * pow(T / I.T0, I.vhs) / (rho * I.R * T);
+        const double T = 0.5 * e2 * irho * I.iCv, iT = 1.0 / T;
+        const double tau = tau_r(I, irho, T, iT);
         const double m3x = M[6] - 2.0 * (M[3] * dx + M[4] * dy) - dx * trM + 2.0 * dd * rho * dx + M[9] - dx * M[8];
         const double m3y = M[7] - 2.0 * (M[4] * dx + M[5] * dy) - dy * trM + 2.0 * dd * rho * dy + M[10] - dy * M[8];
         const double qs = tau / (2.0 * tau + I.hdt * I.Pr);
@@ -841,7 +858,7 @@ __global__ void k32_face_macros(const F32Inst *__restrict__ insts, const int *__
         fm[6] = Cs;
         fm[7] = tau;
         FaceK k;
-        k.e = make_eqp(I, rho, ux, uy, T, qx, qy);
+        k.e = make_eqp_r(I, rho, irho, ux, uy, T, iT * I.iR, qx, qy);
         k.Cs = (float)Cs;
         k.oCs = (float)(1.0 - Cs);
         k.pad0 = 0.f;
@@ -1311,9 +1328,6 @@ __global__ void k32_face_setup(const F32Inst *__restrict__ insts, const int *__r
 // =============================================================================
 // CM: cell macros and evolution constants (one thread per cell, FP64)
 // =============================================================================
-__device__ __forceinline__ double tau_f(const F32Inst &I, double rho, double t) {
-    return I.mu0 * pow(t / I.T0, I.vhs) / (rho * I.R * t);
-}
 
 __global__ void k32_cell_macros(const F32Inst *__restrict__ insts, const int *__restrict__ coff, int ninst, int total) {
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
@@ -1355,13 +1369,15 @@ __global__ void k32_cell_macros(const F32Inst *__restrict__ insts, const int *__
         const double rho_n = I.rho[c], unx = I.u[3 * c], uny = I.u[3 * c + 1], T_n = I.T[c];
         const double qnx = I.q[3 * c], qny = I.q[3 * c + 1];
         const double rhoE_n = rho_n * (0.5 * (unx * unx + uny * uny) + I.Cv * T_n);
-        const double tau_n = tau_f(I, rho_n, T_n);
+        const double irho_n = 1.0 / rho_n, iT_n = 1.0 / T_n;
+        const double tau_n = tau_r(I, irho_n, T_n, iT_n);
         const double rho = rho_n - dt_v * m0;
         const double rux = rho_n * unx - dt_v * m1x, ruy = rho_n * uny - dt_v * m1y;
         const double rhoE = rhoE_n - dt_v * 0.5 * m2;
-        const double ux = rux / rho, uy = ruy / rho;
-        const double T = (rhoE / rho - 0.5 * (ux * ux + uy * uy)) / I.Cv;
-        const double tau = tau_f(I, rho, T);
+        const double irho = 1.0 / rho;
+        const double ux = rux * irho, uy = ruy * irho;
+        const double T = (rhoE * irho - 0.5 * (ux * ux + uy * uy)) * I.iCv, iT = 1.0 / T;
+        const double tau = tau_r(I, irho, T, iT);
         I.rho[c] = rho;
         I.u[3 * c] = ux;
         I.u[3 * c + 1] = uy;
@@ -1369,13 +1385,14 @@ __global__ void k32_cell_macros(const F32Inst *__restrict__ insts, const int *__
         I.T[c] = T;
         I.u32[c] = make_float2((float)ux, (float)uy);
         CellK k;
-        k.en = make_eqp(I, rho_n, unx, uny, T_n, qnx, qny);
-        k.e1 = make_eqp(I, rho, ux, uy, T, qnx, qny);
+        k.en = make_eqp_r(I, rho_n, irho_n, unx, uny, T_n, iT_n * I.iR, qnx, qny);
+        k.e1 = make_eqp_r(I, rho, irho, ux, uy, T, iT * I.iR, qnx, qny);
+        const double itau = 1.0 / tau, itau_n = 1.0 / tau_n;
         k.cm = (float)(I.hdt / (I.hdt - 2.0 * tau_n));
         k.C = (float)(tau / (tau + I.hdt));
-        k.Cs = (float)(I.hdt / (2.0 * tau));
-        k.hdt_tau = (float)(I.hdt / tau);
-        k.hdt_taun = (float)(I.hdt / tau_n);
+        k.Cs = (float)(0.5 * I.hdt * itau);
+        k.hdt_tau = (float)(I.hdt * itau);
+        k.hdt_taun = (float)(I.hdt * itau_n);
         k.dt_v = (float)dt_v;
         I.ck[c] = k;
         // monitor (cdugks_shakhov.cpp:697-719)

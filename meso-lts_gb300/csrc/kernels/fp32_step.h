@@ -71,6 +71,7 @@ struct F32Inst {
     // physics
     double dt, hdt, R, Pr, mu0, vhs, T0, Kd, Cv, gamma, rho0;
     float hdt32, k3_32, twoK32;  // FP32 copies of dt/2, K + 1 and 2K for the velocity loops
+    double iR, iT0, iCv, iRT0, irho0;  // reciprocals of R, T0, Cv, R T0, rho0 (FP64 divisions are slow)
     // reference Maxwellian g0 (rho0, u = 0, T0) and h0 = hm0 g0: the state holds g - g0, h - h0
     double hm0;
     double gmom[10];  // sum w g0 xi^a over the velocity set: 1, x, y, xx, xy, yy, xxx, xxy, xyy, yyy
