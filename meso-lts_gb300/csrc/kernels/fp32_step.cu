@@ -129,7 +129,9 @@ __device__ __forceinline__ EqP make_eqp_r(const F32Inst &I, double rho, double i
     e.ea = (float)(0.5 * (I.iRT0 - iRT));
     e.ebx = (float)(ux * iRT);
     e.eby = (float)(uy * iRT);
-    e.ec = (float)(log(rho * I.irho0 * (I.T0 * I.R * iRT)) - 0.5 * (ux * ux + uy * uy) * iRT);
+    // ln(rho T0 / (rho0 T)) from its argument's offset from 1 (formed in FP64) by the FP32 log1p:
+    // its error is within the FP32 rounding the FP64 logarithm's result would get here
+    e.ec = log1pf((float)(rho * I.irho0 * (I.T0 * I.R * iRT) - 1.0)) - (float)(0.5 * (ux * ux + uy * uy) * iRT);
     e.sg = (float)(c1 * ip * iRT);  // (1 - Pr) / (5 p R T)
     e.sh = (float)(c1 * ip);        // (1 - Pr) / (5 p)
     e.iRT = (float)iRT;
