@@ -201,7 +201,7 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.S[1] = A.alloc<float2>(cv);
         I.u32 = A.alloc<float2>(C);
         I.fk = A.alloc<meso::FaceK>(F);
-        I.fmom = A.alloc<double>((size_t)F * meso::F32_NMOM);
+        I.fmom = A.alloc<float2>((size_t)F * meso::F32_NMOM);
         I.fmac = A.alloc<double>((size_t)F * 8);
         I.fgbar = A.alloc<double>((size_t)F * 4);
         I.fsum = A.alloc<double>((size_t)F * 4);
@@ -212,7 +212,7 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.bnd_g0 = A.alloc<double>(2 * (size_t)std::max(I.nb, 1));
         I.fbar = A.alloc<float2>((size_t)F * NVp);
         I.ck = A.alloc<meso::CellK>(C);
-        I.qpart = A.alloc<double>((size_t)I.ngroup * C * 2);
+        I.qpart = A.alloc<float4>((size_t)I.ngroup * C);
         I.rho = A.alloc<double>(8 * (size_t)C);  // rho, u, T, q contiguous: one copy to the host
         I.u = I.rho + C;
         I.T = I.rho + 4 * (size_t)C;

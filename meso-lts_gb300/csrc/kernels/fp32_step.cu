@@ -207,7 +207,7 @@ template <int N> __device__ __forceinline__ void warp_sum(float (&v)[N]) {
 // renormalises, so the result carries about 44 significant bits (the pair's precision) at FP32
 // instruction rates.  Every lane of a group receives the same, order-independent-of-lane value;
 // the FP64 result is hi + lo.  All 32 lanes of the warp must call it.
-template <int W = 32> __device__ __forceinline__ double warp_sum_ff(float hi, float lo) {
+template <int W = 32> __device__ __forceinline__ float2 warp_sum_ff2(float hi, float lo) {
 #pragma unroll
     for (int o = W / 2; o > 0; o >>= 1) {
         const float bh = __shfl_xor_sync(0xffffffffu, hi, o), bl = __shfl_xor_sync(0xffffffffu, lo, o);
@@ -218,8 +218,21 @@ template <int W = 32> __device__ __forceinline__ double warp_sum_ff(float hi, fl
         hi = __fadd_rn(sum, l);
         lo = __fsub_rn(l, __fsub_rn(hi, sum));
     }
-    return (double)hi + (double)lo;
+    return make_float2(hi, lo);
 }
+template <int W = 32> __device__ __forceinline__ double warp_sum_ff(float hi, float lo) {
+    const float2 r = warp_sum_ff2<W>(hi, lo);
+    return (double)r.x + (double)r.y;
+}
+
+// A double as an unevaluated float pair (hi + lo, about 48 significant bits), and back: FP64
+// results that a warp holds in every lane are stored as pairs and combined by the one thread per
+// face or cell that uses them.
+__device__ __forceinline__ float2 split_ff(double v) {
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+__device__ __forceinline__ double join_ff(float2 v) { return (double)v.x + (double)v.y; }
 
 template <int N> __device__ __forceinline__ float pick(const float (&v)[N], int lane) {
     float r = 0.f;
@@ -556,7 +569,7 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
         const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
         const int ch0 = grp * cpg, ch1 = min(I.chunks, ch0 + cpg);
         if (ch0 >= ch1) {  // an empty velocity group (not planned, see build_fp32_instance) adds nothing
-            for (int c = threadIdx.x; c < 2 * nc; c += kUT) I.qpart[((size_t)grp * I.C + cs) * 2 + c] = 0.0;
+            for (int c = threadIdx.x; c < nc; c += kUT) I.qpart[(size_t)grp * I.C + cs + c] = make_float4(0.f, 0.f, 0.f, 0.f);
             continue;
         }
         const float2 *__restrict__ S = I.S[cur];
@@ -653,11 +666,8 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
         for (int r = 0; r < RC; ++r) {  // one float-float warp reduction per cell and item
             const int cl = warp + kUW * r;
             if (cl >= nc) break;
-            const double q0 = warp_sum_ff(qs[r][0], -qc[r][0]), q1 = warp_sum_ff(qs[r][1], -qc[r][1]);
-            if (lane == 0) {
-                I.qpart[((size_t)grp * I.C + cs + cl) * 2] = q0;
-                I.qpart[((size_t)grp * I.C + cs + cl) * 2 + 1] = q1;
-            }
+            const float2 q0 = warp_sum_ff2(qs[r][0], -qc[r][0]), q1 = warp_sum_ff2(qs[r][1], -qc[r][1]);
+            if (lane == 0) I.qpart[(size_t)grp * I.C + cs + cl] = make_float4(q0.x, q0.y, q1.x, q1.y);
         }
         __syncthreads();
     }
@@ -736,7 +746,7 @@ __global__ void __launch_bounds__(256) k32_face_moments(const F32Inst *__restric
 #pragma unroll
             for (int k = 1; k < F32_NMOM; ++k)
                 if (lane == k) mine = M[k];
-            I.fmom[(size_t)f * F32_NMOM + lane] = mine;
+            I.fmom[(size_t)f * F32_NMOM + lane] = split_ff(mine);
         }
     }
 }
@@ -803,14 +813,14 @@ __global__ void __launch_bounds__(256) k32_face_moments_small(const F32Inst *__r
                 for (int k = 0; k < F32_NMOM; ++k) kahan(s[k], c[k], m[k]);
             }
         }
-        double M[F32_NMOM];
+        float2 M[F32_NMOM];
 #pragma unroll
-        for (int k = 0; k < F32_NMOM; ++k) M[k] = warp_sum_ff<L>(s[k], -c[k]);
+        for (int k = 0; k < F32_NMOM; ++k) M[k] = warp_sum_ff2<L>(s[k], -c[k]);
         if (on) {
 #pragma unroll
             for (int k0 = 0; k0 < F32_NMOM; k0 += L) {
                 const int k = k0 + sl;
-                double mine = 0.0;
+                float2 mine = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int q = 0; q < F32_NMOM; ++q)
                     if (q == k) mine = M[q];
@@ -831,7 +841,7 @@ __global__ void k32_face_macros(const F32Inst *__restrict__ insts, const int *__
         const float2 uo = I.u32[I.fown[f]], un = I.u32[I.fnei[f]];
         const double u0x = (double)(0.5f * (uo.x + un.x)), u0y = (double)(0.5f * (uo.y + un.y));
         double M[F32_NMOM];
-        for (int k = 0; k < F32_NMOM; ++k) M[k] = I.fmom[(size_t)f * F32_NMOM + k];
+        for (int k = 0; k < F32_NMOM; ++k) M[k] = join_ff(I.fmom[(size_t)f * F32_NMOM + k]);
         {  // the reference pair's part of the moments, exactly in FP64
             double M0[F32_NMOM];
             g0_raw_moments(I, u0x, u0y, M0);
@@ -1424,8 +1434,9 @@ __global__ void k32_heat_flux(const F32Inst *__restrict__ insts, const int *__re
         const int c = g - coff[i];
         double qx = 0.0, qy = 0.0;
         for (int grp = 0; grp < I.ngroup; ++grp) {
-            qx += I.qpart[((size_t)grp * I.C + c) * 2];
-            qy += I.qpart[((size_t)grp * I.C + c) * 2 + 1];
+            const float4 qp = I.qpart[(size_t)grp * I.C + c];
+            qx += (double)qp.x + (double)qp.y;
+            qy += (double)qp.z + (double)qp.w;
         }
         {  // the reference pair's part, 1/2 sum w c (c^2 g0 + h0) about the cell velocity
             double M0[F32_NMOM];

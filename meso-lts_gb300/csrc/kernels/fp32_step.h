@@ -109,7 +109,7 @@ struct F32Inst {
     float2 *S[2];          // [C][NVp] (g - g0, h - h0) ping-pong; S[status->step & 1] is current
     float2 *u32;           // [C] cell velocity (FP32) = reference velocity of the face moments
     FaceK *fk;             // [F]
-    double *fmom;          // [F][11] raw face moments of the reconstruction (deviation part)
+    float2 *fmom;          // [F][11] raw face moments of the reconstruction (deviation part), float pairs
     double *fmac;          // [F][8] rho, ux, uy, T, qx, qy, Cs, tau
     double *fgbar;         // [F][4] fluxes of the reconstructed values (mass, mom x, mom y, energy) per unit area along n0
     double *fsum;          // [F][4] same for the face equilibrium (interior) or the final boundary values
@@ -118,7 +118,7 @@ struct F32Inst {
     float2 *fbar;              // [F][NVp] reconstructed interior face values (moments -> update kernel)
     double *bnd_g0;            // [nb][2] half-range sums of g0 (fp32_prepare)
     CellK *ck;             // [C]
-    double *qpart;         // [ngroup][C][2]
+    float4 *qpart;         // [ngroup][C] heat-flux partials (qx, qy) as float pairs
     double *rho, *u, *T, *q;   // [C], [3C], [C], [3C]
     double *fm0, *fm1, *fm2;   // flux moments
     int *repair_list;
