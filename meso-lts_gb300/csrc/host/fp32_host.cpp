@@ -278,7 +278,7 @@ int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso
     for (const int2 &it : items) n2 += insts[it.x].vpl == 2 ? 1 : 0;
     // boundary faces: one block per face for large velocity sets, eight faces (a warp each) per
     // block for small ones
-    std::vector<int2> bblocks;
+    std::vector<int2> bblocks, bblk;
     for (int i = 0; i < n; ++i) {
         const auto &I = insts[i];
         if (I.NVp <= meso::F32_SMALL_NVP) s.has_small = 1;
@@ -286,8 +286,10 @@ int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso
         if (I.NVp <= meso::F32_SMALL_NVP)
             for (int b = 0; b < I.nb; b += 8) bblocks.push_back(make_int2(i, -b - 1));
         else
-            for (int b = 0; b < I.nb; ++b) bblocks.push_back(make_int2(i, b));
+            for (int b = 0; b < I.nb; ++b) bblk.push_back(make_int2(i, b));
     }
+    const int nbw = (int)bblocks.size();
+    bblocks.insert(bblocks.end(), bblk.begin(), bblk.end());
     auto put = [&](const void *src, size_t bytes) -> void * {
         void *p = nullptr;
         if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) return nullptr;
@@ -304,6 +306,7 @@ int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso
     if (!s.d_inst || !s.d_items || !s.d_face_items || !s.d_cell_items || !s.d_bnd_items || !s.d_bnd_blocks)
         return -1;
     s.nbnd_blocks = (int)bblocks.size();
+    s.nbnd_warp = nbw;
     s.ninst = n;
     s.nitems = (int)items.size();
     s.nitems_vpl2 = n2;

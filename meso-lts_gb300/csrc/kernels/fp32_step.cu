@@ -1249,20 +1249,22 @@ template <int TPF> __device__ __forceinline__ void bnd_face(const F32Inst &I, in
     G::sync();  // the group's shared scalars are rewritten by its next face
 }
 
-// Work items (instance, first boundary face): y >= 0 is one face for the whole block, y < 0 is
-// the eight faces -y - 1 ... -y + 6 of the instance, one per warp.
+// Work items (instance, first boundary face): for TPF = kBndThreads (large velocity sets) y is
+// one face for the whole block; for TPF = 32 (small sets) y = -(first face) - 1 of the eight faces
+// the block's warps take, one each.  Two kernels, so that each form gets its own register budget.
+template <int TPF>
 __global__ void __launch_bounds__(kBndThreads) k32_boundary(const F32Inst *__restrict__ insts,
                                                            const int2 *__restrict__ items, int nitems) {
-    __shared__ BndShared sh[kBndThreads / 32];
+    __shared__ BndShared sh[TPF == 32 ? kBndThreads / 32 : 1];
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 item = items[it];
         const F32Inst &I = insts[item.x];
         if (step_stopped(I.status)) continue;
-        if (item.y >= 0) {
-            bnd_face<kBndThreads>(I, item.y, sh[0]);
-        } else {
+        if (TPF == 32) {
             const int b = -item.y - 1 + (threadIdx.x >> 5);
             if (b < I.nb) bnd_face<32>(I, b, sh[threadIdx.x >> 5]);
+        } else {
+            bnd_face<kBndThreads>(I, item.y, sh[0]);
         }
     }
 }
@@ -1700,12 +1702,26 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     k32_face_macros<<<grid_of(s.total_faces, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_face_items, s.ninst,
                                                                           s.total_faces);
     mark(2);
+    auto boundary = [&](cudaStream_t st) {  // warp-per-face items first, then block-per-face items
+        int k = 0;
+        if (s.nbnd_warp > 0) {
+            k32_boundary<32><<<grid_of(s.nbnd_warp, 1, cap), kBndThreads, 0, st>>>(s.d_inst, s.d_bnd_blocks,
+                                                                                   s.nbnd_warp);
+            ++k;
+        }
+        if (s.nbnd_blocks > s.nbnd_warp) {
+            k32_boundary<kBndThreads><<<grid_of(s.nbnd_blocks - s.nbnd_warp, 1, cap), kBndThreads, 0, st>>>(
+                s.d_inst, s.d_bnd_blocks + s.nbnd_warp, s.nbnd_blocks - s.nbnd_warp);
+            ++k;
+        }
+        return k;
+    };
     const bool branch = fork && !ev && s.total_bnd > 0;
+    int nbl = 0;
     if (branch) {  // boundary faces on the side stream, interior faces' equilibrium fluxes here
         cudaEventRecord(fork->fork, stream);
         cudaStreamWaitEvent(fork->side, fork->fork, 0);
-        k32_boundary<<<grid_of(s.nbnd_blocks, 1, cap), kBndThreads, 0, fork->side>>>(s.d_inst, s.d_bnd_blocks,
-                                                                                     s.nbnd_blocks);
+        nbl = boundary(fork->side);
         cudaEventRecord(fork->join, fork->side);
     }
     if (s.has_large)
@@ -1719,11 +1735,9 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     n += 3;
     if (branch) {
         cudaStreamWaitEvent(stream, fork->join, 0);
-        ++n;
+        n += nbl;
     } else if (s.total_bnd > 0) {
-        k32_boundary<<<grid_of(s.nbnd_blocks, 1, cap), kBndThreads, 0, stream>>>(s.d_inst, s.d_bnd_blocks,
-                                                                                 s.nbnd_blocks);
-        ++n;
+        n += boundary(stream);
     }
     mark(4);
     k32_cell_macros<<<grid_of(s.total_cells, 128, cap), 128, 0, stream>>>(s.d_inst, s.d_cell_items, s.ninst,

@@ -138,8 +138,8 @@ struct Fp32State {
     int *d_face_items = nullptr; // prefix sums of faces / cells / boundary faces over instances
     int *d_cell_items = nullptr;
     int *d_bnd_items = nullptr;
-    int2 *d_bnd_blocks = nullptr; // boundary-kernel blocks: (inst, face b) or (inst, -(first of 8 faces) - 1)
-    int nbnd_blocks = 0;
+    int2 *d_bnd_blocks = nullptr; // boundary-kernel blocks: (inst, -(first of 8 faces) - 1), then (inst, face b)
+    int nbnd_blocks = 0, nbnd_warp = 0;  // the first nbnd_warp items are warp-per-face items
     int has_small = 0, has_large = 0;  // instances with NVp <= / > F32_SMALL_NVP
     int total_faces = 0, total_cells = 0, total_bnd = 0;
     int num_sms = 0;
