@@ -325,21 +325,35 @@ def run_batched(tmp: str, steps: int = 20, warm: int = 3, autotune: bool = True)
                 best, ms = mg.autotune(path, steps=3)
                 tuned[key] = (best.tile_cells, best.vpl, best.ngroup, round(ms, 4))
     tune_s = time.perf_counter() - t0
-    members = []
-    for inst, path in zip(insts, paths):
+    # the same instances stepped one at a time, each with its tuned shape (device time per step, summed)
+    alone_ms = 0.0
+    for path in paths:
         case = mg.Case(path)
         rho, u, T, mask = case.initial_fields()
         s = mg.Solver(case=case, precision=mg.FP32, mask=mask)
         s.init_macros(rho, u, T, None, 0)
-        members.append((case, s))
-    setup_s = time.perf_counter() - t0
-    dev_bytes = sum(s.device_bytes() for _, s in members)
-    # the same instances stepped one at a time (device time per step, summed)
-    alone_ms = 0.0
-    for case, s in members:
         s.step(1)
         s.step(3)
         alone_ms += s.last_step_ms() / 3
+        s.close()
+        case.close()
+    # batch members: the tuned tile size and velocities per lane, one velocity group per tile (the
+    # batch supplies the parallelism that the groups give a solve alone)
+    members = []
+    for inst, path in zip(insts, paths):
+        case = mg.Case(path)
+        rho, u, T, mask = case.initial_fields()
+        prm = case.params
+        prm.precision = mg.FP32
+        key = (inst["side"], inst["dvs"])
+        if key in tuned:
+            prm.tile_cells, prm.vpl = tuned[key][0], tuned[key][1]
+        prm.ngroup = 1
+        s = mg.Solver(case=case, precision=mg.FP32, mask=mask, params=prm)
+        s.init_macros(rho, u, T, None, 0)
+        members.append((case, s))
+    setup_s = time.perf_counter() - t0
+    dev_bytes = sum(s.device_bytes() for _, s in members)
     b = mg.Batch([s for _, s in members])
     b.step(warm)
     before = [s.status().step for _, s in members]

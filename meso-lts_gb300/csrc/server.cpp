@@ -195,6 +195,9 @@ int meso_server_submit(meso_server *s, const char *case_file, const meso_params 
     if (params) p = *params;
     p.precision = MESO_FP32;
     if (p.solver != MESO_SOLVER_CDUGKS_SHAKHOV) return fail(MESO_ERR_UNSUPPORTED, "served solves are FP32 Shakhov solves");
+    // One velocity group per tile unless the request sets a shape: the batch of running solves
+    // supplies the parallelism, and whole-velocity-range items carry the least per-item overhead.
+    if (p.tile_cells == 0 && p.vpl == 0 && p.ngroup == 0) p.ngroup = 1;
     r->params = p;
     int32_t ws = 0, rnp = 0, ol = 0, onp = 0;
     meso_case_loop_settings(r->kase, &r->max_step, &ws, &rnp, &ol, &onp);

@@ -24,6 +24,7 @@ def _params(path, interval, limit, fields=0):
     p.residual_interval = interval
     p.residual_limit = limit
     p.residual_fields = fields
+    p.ngroup = 1  # the server's own choice for requests that set no kernel shape
     return p
 
 

@@ -42,10 +42,13 @@ def _poison(rt, sizes=(4 << 10, 16 << 10, 64 << 10, 256 << 10, 1 << 20, 4 << 20)
         rt.cudaFree(p)
 
 
-def _run(path, steps):
+def _run(path, steps, ngroup=0):
     case = mg.Case(path)
     rho, u, T, mask = case.initial_fields()
-    s = mg.Solver(case=case, precision=mg.FP32, mask=mask)
+    prm = case.params
+    prm.precision = mg.FP32
+    prm.ngroup = ngroup
+    s = mg.Solver(case=case, precision=mg.FP32, mask=mask, params=prm)
     s.init_macros(rho, u, T, None, 0)
     s.step(steps)
     out, st = s.macros(case.ncell), s.status()
@@ -76,10 +79,18 @@ def test_served_solves_on_reused_memory_equal_alone(gpu, tmp_path):
         side = (16, 24)[i % 2]
         paths.append(cases.shakhov_cavity(str(tmp_path / f"r{i}"), "quad", side, "hgh", 28, 0.1 + 0.01 * i, 0.12, 60,
                                           cfl=0.5))
+    # six velocity groups over the 13 chunks of hGH 28^2 (planned as five): the split that once
+    # left a group without chunks
+    def prm(path):
+        q = mg.Case(path).params
+        q.precision = mg.FP32
+        q.ngroup = 6
+        return q
+
     srv = mg.Server(hbm_budget_bytes=8 << 30, max_members=4)
     tags, got = {}, {}
     for i, p in enumerate(paths):
-        tags[srv.submit(p)] = i
+        tags[srv.submit(p, prm(p))] = i
         for t in srv.poll(20):
             got[tags[t]] = srv.result(t)
     for _ in range(200):
@@ -91,7 +102,7 @@ def test_served_solves_on_reused_memory_equal_alone(gpu, tmp_path):
     assert len(got) == len(paths)
     for i, p in enumerate(paths):
         (rho, u, T, q), st, _ = got[i]
-        ref, st_ref = _run(p, 60)
+        ref, st_ref = _run(p, 60, ngroup=6)
         assert st.step == st_ref.step == 60 and st.run_state == st_ref.run_state, i
         for k, x, y in zip(("rho", "u", "T", "q"), (rho, u, T, q), ref):
             assert np.array_equal(x, y), (i, k)
