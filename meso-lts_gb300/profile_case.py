@@ -6,7 +6,8 @@
 Builds the workload's case files (cases.py) in a temporary directory, creates
 a context, runs initial() and N steps, prints the mean device time per step.
 served64 is a batch of the first 64 requests of the served stream (FP32 cavities of
-sides 16-32, hGH 28^2 or NC 21^2 velocities) stepped as one batch.  --phases
+sides 16-32, hGH 28^2 or NC 21^2 velocities, one velocity group per tile as the
+server runs them) stepped as one batch.  --phases
 also prints the mean device time of each kernel phase (kernels launched one by
 one, a few more steps).
 Meant to be wrapped by ncu, e.g.
@@ -61,7 +62,10 @@ def served_batch(a) -> int:
         for r in cases.config5_requests(count=64):
             case = mg.Case(cases.config5_case(os.path.join(d, f"s{r['index']}"), r, 8000))
             rho, u, T, mask = case.initial_fields()
-            s = mg.Solver(case=case, precision=mg.FP32, mask=mask)
+            prm = case.params
+            prm.precision = mg.FP32
+            prm.ngroup = 1  # as the server runs requests that set no kernel shape
+            s = mg.Solver(case=case, precision=mg.FP32, mask=mask, params=prm)
             s.init_macros(rho, u, T, None, 0)
             solvers.append(s)
             work += case.ncell * case.nv
