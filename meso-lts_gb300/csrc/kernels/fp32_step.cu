@@ -108,10 +108,10 @@ __device__ __forceinline__ float2 dshakhov(const EqP &e, float xx, float xy, flo
     const float gm = g0 + dgm;
     const float cx = xx - e.ux, cy = xy - e.uy;
     const float cc = fmaf(cx, cx, cy * cy);
-    const float cq = fmaf(cx, e.qx, cy * e.qy);
-    const float t = cc * e.iRT;
-    const float dg = fmaf(gm * (e.sg * cq), t - 4.0f, dgm);
-    const float dh = fmaf(gm * (e.sh * cq), fmaf(t - 2.0f, k3, -twoK), fmaf(e.hm, dgm, e.dhm * g0));
+    const float a = gm * fmaf(cx, e.qgx, cy * e.qgy);  // g_M (1 - Pr) (c.q) / (5 p R T)
+    const float dg = fmaf(a, fmaf(cc, e.iRT, -4.0f), dgm);
+    // (c^2 / RT - 2)(K + 1) - 2K = c^2 (K + 1) / RT - 2 (K + 1) - 2K
+    const float dh = fmaf(a * e.RT, fmaf(cc, e.iRTk3, fmaf(-2.0f, k3, -twoK)), fmaf(e.hm, dgm, e.dhm * g0));
     return make_float2(dg, dh);
 }
 
@@ -124,17 +124,18 @@ __device__ __forceinline__ EqP make_eqp_r(const F32Inst &I, double rho, double i
     EqP e;
     e.ux = (float)ux;
     e.uy = (float)uy;
-    e.qx = (float)qx;
-    e.qy = (float)qy;
+    const double sg = c1 * ip * iRT;  // (1 - Pr) / (5 p R T)
+    e.qgx = (float)(sg * qx);
+    e.qgy = (float)(sg * qy);
     e.ea = (float)(0.5 * (I.iRT0 - iRT));
     e.ebx = (float)(ux * iRT);
     e.eby = (float)(uy * iRT);
     // ln(rho T0 / (rho0 T)) from its argument's offset from 1 (formed in FP64) by the FP32 log1p:
     // its error is within the FP32 rounding the FP64 logarithm's result would get here
     e.ec = log1pf((float)(rho * I.irho0 * (I.T0 * I.R * iRT) - 1.0)) - (float)(0.5 * (ux * ux + uy * uy) * iRT);
-    e.sg = (float)(c1 * ip * iRT);  // (1 - Pr) / (5 p R T)
-    e.sh = (float)(c1 * ip);        // (1 - Pr) / (5 p)
+    e.RT = (float)RT;
     e.iRT = (float)iRT;
+    e.iRTk3 = (float)((I.Kd + 1.0) * iRT);
     e.hm = (float)((I.Kd + 1.0) * RT);
     e.dhm = (float)((I.Kd + 1.0) * I.R * (T - I.T0));
     return e;

@@ -33,13 +33,14 @@ constexpr int F32_SMALL_NVP = 2048;  // velocity sets up to this size: a warp pe
 // so that E, and with it g_M - g0 = g0 expm1(E), carries the rounding of the
 // deviation only.
 struct EqP {
-    float ux, uy, qx, qy;
+    float ux, uy;
+    float qgx, qgy;  // q (1 - Pr) / (5 p R T): the Shakhov factor of g folded into q
     float ea, ebx, eby, ec;
-    float sg;   // (1 - Pr) / (5 p R T)
-    float sh;   // (1 - Pr) / (5 p)
-    float iRT;  // 1 / (R T)
-    float hm;   // (K + 3 - D) R T
-    float dhm;  // (K + 3 - D) R (T - T0)
+    float RT;     // R T: the h factor over the g factor
+    float iRT;    // 1 / (R T)
+    float iRTk3;  // (K + 1) / (R T)
+    float hm;     // (K + 3 - D) R T
+    float dhm;    // (K + 3 - D) R (T - T0)
 };
 
 // Residual check state of one instance (the reference's Res[...] print list and converge counter,
