@@ -74,6 +74,39 @@ __device__ __forceinline__ double h_shakhov(const KParams &k, double rho, double
 __device__ __forceinline__ double tau_f(const KParams &k, double rho, double t) {
     return k.mu0 * pow(t / k.T0, k.vhs) / (rho * k.R * t);
 }
+
+// The Shakhov equilibrium of one (rho, T) with its per-state factors formed once, so that the
+// velocity loops evaluate g_maxwell, g_shakhov and h_shakhov (cdugks_shakhov.cpp:185-211) with one
+// exp and no division per velocity (FP64 divisions are slow on this GPU).  Same formulas; the
+// results differ from the per-velocity divisions in the last bits only.
+struct EqK64 {
+    double A;     // rho / (2 pi R T)^(D/2)
+    double oRT2;  // 1 / (2 R T)
+    double iRT;   // 1 / (R T)
+    double sg;    // (1 - Pr) / (5 p R T)
+    double sh;    // (1 - Pr) / (5 p)
+    double hm;    // (K + 3 - D) R T
+};
+template <int DIM> __device__ __forceinline__ EqK64 make_eqk(const KParams &k, double rho, double t) {
+    EqK64 e;
+    const double RT = k.R * t;
+    e.iRT = 1.0 / RT;
+    e.oRT2 = 0.5 * e.iRT;
+    e.A = DIM == 2 ? rho * e.oRT2 / kPI : rho / pow(2.0 * kPI * RT, 1.5);
+    const double c1 = (1.0 - k.Pr) / 5.0, ip = e.iRT / rho;
+    e.sg = c1 * ip * e.iRT;
+    e.sh = c1 * ip;
+    e.hm = (k.Kd + 3.0 - k.Dd) * RT;
+    return e;
+}
+// g_S and h_S at one velocity (cc = |c|^2, cq = c.q)
+__device__ __forceinline__ void shakhov_eq(const KParams &k, const EqK64 &e, double cc, double cq, double &gs,
+                                           double &hs) {
+    const double gm = e.A * exp(-cc * e.oRT2);
+    const double t = cc * e.iRT;
+    gs = (e.sg * cq) * (t - k.Dd - 2.0) * gm + gm;
+    hs = (e.sh * cq) * ((t - k.Dd) * (k.Kd + 3.0 - k.Dd) - 2.0 * k.Kd) * gm + e.hm * gm;
+}
 template <int DIM> __device__ __forceinline__ double f_maxwell(const KParams &k, double rho, V3 u, V3 xi) {
     double ku_RT = dot<DIM>(u, xi) * k.over_RT;
     double uu_RT = dot<DIM>(u, u) * k.over_RT;
@@ -315,13 +348,13 @@ __global__ void __launch_bounds__(kBlock) k_face_eq(DMesh m, KParams k, const DS
     const double qs = tau / (2.0 * tau + k.hdt * k.Pr);
     const V3 q = v3(m3[0] * qs, m3[1] * qs, m3[2] * qs);
     const double C_s = k.hdt / (2.0 * tau + k.hdt);
+    const EqK64 e = make_eqk<DIM>(k, rho, T);
     for (int p = lane; p < m.NV; p += L) {
         const V3 c = xi_of(m, p) - u;
         const double cc = dot<DIM>(c, c);
         const double cq = dot<DIM>(c, q);
-        const double g_m = g_maxwell<DIM>(k, rho, T, cc);
-        const double g_s = g_shakhov(k, rho, T, cc, cq, g_m);
-        const double h_s = h_shakhov(k, rho, T, cc, cq, g_m);
+        double g_s, h_s;
+        shakhov_eq(k, e, cc, cq, g_s, h_s);
         face0[base + p] = (1.0 - C_s) * face0[base + p] + C_s * g_s;
         face1[base + p] = (1.0 - C_s) * face1[base + p] + C_s * h_s;
     }
@@ -587,6 +620,8 @@ __global__ void __launch_bounds__(kBlock) k_update_shakhov(DMesh m, KParams k, D
     const double cm = k.hdt / (k.hdt - 2.0 * tau_n);
     const double Cc = tau / (tau + k.hdt);
     const double C_s = k.hdt / (2.0 * tau);
+    const double itau = 1.0 / tau, itau_n = 1.0 / tau_n;
+    const EqK64 e_n = make_eqk<DIM>(k, rho_n, T_n), e1 = make_eqk<DIM>(k, rho, T);
     double m3[3] = {0, 0, 0};
     if (active)
         for (int p = lane; p < m.NV; p += L) {
@@ -594,19 +629,17 @@ __global__ void __launch_bounds__(kBlock) k_update_shakhov(DMesh m, KParams k, D
             const V3 c_n = xi - u_n;
             const double cc_n = dot<DIM>(c_n, c_n);
             const double cq_n = dot<DIM>(c_n, q_n);
-            const double g_m_n = g_maxwell<DIM>(k, rho_n, T_n, cc_n);
-            const double g_s_n = g_shakhov(k, rho_n, T_n, cc_n, cq_n, g_m_n);
-            const double h_s_n = h_shakhov(k, rho_n, T_n, cc_n, cq_n, g_m_n);
+            double g_s_n, h_s_n;
+            shakhov_eq(k, e_n, cc_n, cq_n, g_s_n, h_s_n);
             const double g_n = cm * g_s_n + (1.0 - cm) * g_cell[base + p];
             const double h_n = cm * h_s_n + (1.0 - cm) * h_cell[base + p];
             const V3 cv = xi - u;
             const double cc = dot<DIM>(cv, cv);
             const double cq = dot<DIM>(cv, q_n);
-            const double g_m = g_maxwell<DIM>(k, rho, T, cc);
-            const double g_s = g_shakhov(k, rho, T, cc, cq, g_m);
-            const double h_s = h_shakhov(k, rho, T, cc, cq, g_m);
-            const double g = Cc * (g_n + k.hdt * (g_s / tau + (g_s_n - g_n) / tau_n) - dt_v * flux_g[base + p]);
-            const double h = Cc * (h_n + k.hdt * (h_s / tau + (h_s_n - h_n) / tau_n) - dt_v * flux_h[base + p]);
+            double g_s, h_s;
+            shakhov_eq(k, e1, cc, cq, g_s, h_s);
+            const double g = Cc * (g_n + k.hdt * (g_s * itau + (g_s_n - g_n) * itau_n) - dt_v * flux_g[base + p]);
+            const double h = Cc * (h_n + k.hdt * (h_s * itau + (h_s_n - h_n) * itau_n) - dt_v * flux_h[base + p]);
             const double hw = 0.5 * m.w[p];
             const double s = cc * g + h;
             m3[0] += (cv.x * hw) * s;
