@@ -229,8 +229,10 @@ def run_reference(args, rank: int, dist: Dist) -> None:
     with tempfile.TemporaryDirectory() as tmp:
         path = build_workload(tmp, "fp64")
         threads = os.cpu_count() or 1
-        steps = max(1, min(args.steps, 3))
-        warm = 1 if args.warmup > 0 else 0
+        # bounded: a config-2 step takes about 0.7 s on 16 Grace cores, so at most 10 timed steps
+        # after 3 to 5 warm-up steps keep the run within a few minutes on any host
+        steps = max(1, min(args.steps, 10))
+        warm = max(3, min(args.warmup, 5))
         import meso_gpu as mg
         import meso_oracle as mo
 
@@ -238,8 +240,7 @@ def run_reference(args, rank: int, dist: Dist) -> None:
         rho, u, T, mask = case.initial_fields()
         o = mo.Oracle(case, threads, mask)
         o.init(rho, u, T, None, 0)
-        if warm:
-            o.step(warm)
+        o.step(warm)
         t0 = time.perf_counter()
         done, _ = o.step(steps)
         secs = time.perf_counter() - t0
