@@ -1774,10 +1774,5 @@ int fp32_init(const Fp32State &s, int mode, cudaStream_t stream) {
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int fp32_finalize_q(const Fp32State &s, cudaStream_t stream) {
-    (void)s;
-    (void)stream;
-    return 0;
-}
 
 }  // namespace meso

@@ -164,6 +164,5 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
 // Once per instance set-up, after the instances are on the device.
 int fp32_prepare(const Fp32State &s, cudaStream_t stream);
 int fp32_init(const Fp32State &s, int mode, cudaStream_t stream);
-int fp32_finalize_q(const Fp32State &s, cudaStream_t stream);
 
 }  // namespace meso
