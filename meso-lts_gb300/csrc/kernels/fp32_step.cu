@@ -309,6 +309,8 @@ template <int VPL> struct __align__(128) UpdSmem {
     float2 fv[2][F32_MAX_TF * SEG];             // (n0.xi) A f_face of each tile face (cp.async target)
     const float2 *src[F32_MAX_TF];              // where each tile face's flux values are, [NVp]
     CellK ck[F32_MAX_CELLS];
+    int4 c4o[F32_MAX_CELLS];                    // cells with four faces: their faces' offsets into fv
+    float4 c4s[F32_MAX_CELLS];                  // and signs (-1 where the cell is the face's neighbour)
     int cf_off[F32_MAX_CELLS + 1];
     unsigned char cft[F32_MAX_CF];              // per cell-face entry: tile face | 0x80 if the cell is its neighbour
     int nc, ntf, cs;
@@ -583,6 +585,19 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
         for (int c = threadIdx.x; c <= nc; c += kUT) sm.cf_off[c] = I.cf_ptr[cs + c] - j0;
         const int ncf = I.cf_ptr[cs + nc] - j0;
         for (int e = threadIdx.x; e < ncf; e += kUT) sm.cft[e] = I.cf_tf[j0 + e];
+        for (int c = threadIdx.x; c < nc; c += kUT) {  // four-face cells decoded once per item
+            const int e0 = I.cf_ptr[cs + c] - j0;
+            if (I.cf_ptr[cs + c + 1] - j0 - e0 != 4) continue;
+            int o[4];
+            float g[4];
+            for (int q = 0; q < 4; ++q) {
+                const unsigned char t = I.cf_tf[j0 + e0 + q];
+                o[q] = (t & 0x7f) * SEG;
+                g[q] = (t & 0x80) ? -1.f : 1.f;
+            }
+            sm.c4o[c] = make_int4(o[0], o[1], o[2], o[3]);
+            sm.c4s[c] = make_float4(g[0], g[1], g[2], g[3]);
+        }
         const int q0 = I.tile_tf_ptr[tile], ntf = I.tile_tf_ptr[tile + 1] - q0;
         for (int q = threadIdx.x; q < ntf; q += kUT) {
             const int f = I.tf_face[q0 + q], b = I.fbnd[f];
@@ -625,17 +640,30 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
                 float fg[VPL], fh[VPL];
 #pragma unroll
                 for (int v = 0; v < VPL; ++v) fg[v] = fh[v] = 0.f;
-                const int e1 = sm.cf_off[cl + 1];
-#pragma unroll 4
-                for (int e = sm.cf_off[cl]; e < e1; ++e) {  // outward flux of the cell (:616-629)
-                    const unsigned char t = sm.cft[e];
-                    const float2 *ff = sm.fv[buf] + (t & 0x7f) * SEG + lane;
-                    const float sgn = (t & 0x80) ? -1.f : 1.f;
+                const int e0 = sm.cf_off[cl], e1 = sm.cf_off[cl + 1];
+                if (e1 - e0 == 4) {  // outward flux of the cell (:616-629), the four faces in entry order
+                    const int4 o = sm.c4o[cl];
+                    const float4 g = sm.c4s[cl];
+                    const float2 *ff = sm.fv[buf] + lane;
 #pragma unroll
                     for (int v = 0; v < VPL; ++v) {
-                        const float2 val = ff[v * 32];
-                        fg[v] = fmaf(sgn, val.x, fg[v]);
-                        fh[v] = fmaf(sgn, val.y, fh[v]);
+                        const float2 a = ff[o.x + v * 32], b = ff[o.y + v * 32], c = ff[o.z + v * 32],
+                                     d = ff[o.w + v * 32];
+                        fg[v] = fmaf(g.w, d.x, fmaf(g.z, c.x, fmaf(g.y, b.x, fmaf(g.x, a.x, fg[v]))));
+                        fh[v] = fmaf(g.w, d.y, fmaf(g.z, c.y, fmaf(g.y, b.y, fmaf(g.x, a.y, fh[v]))));
+                    }
+                } else {
+#pragma unroll 4
+                    for (int e = e0; e < e1; ++e) {
+                        const unsigned char t = sm.cft[e];
+                        const float2 *ff = sm.fv[buf] + (t & 0x7f) * SEG + lane;
+                        const float sgn = (t & 0x80) ? -1.f : 1.f;
+#pragma unroll
+                        for (int v = 0; v < VPL; ++v) {
+                            const float2 val = ff[v * 32];
+                            fg[v] = fmaf(sgn, val.x, fg[v]);
+                            fh[v] = fmaf(sgn, val.y, fh[v]);
+                        }
                     }
                 }
                 const CellK k = sm.ck[cl];
