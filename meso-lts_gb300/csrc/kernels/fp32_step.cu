@@ -283,6 +283,8 @@ template <int VPL> struct __align__(128) TileSmem {
     float2 phi[2][F32_MAX_SLOTS * SEG];         // double-buffered chunk of the tile + halo (cp.async target)
     float4 G[F32_MAX_GSLOTS * SEG];             // gradients (g_x, g_y, h_x, h_y) of tile + 1-ring cells
     float2 ga[F32_MAX_GENT];                    // gradient stencil coefficients
+    int4 g4o[F32_MAX_GSLOTS];                   // slots with four stencil entries: neighbour offsets into phi
+    float4 g4x[F32_MAX_GSLOTS], g4y[F32_MAX_GSLOTS];  // and their coefficients
     uint2 cls[2][F32_MAX_OWNED * VPL];          // upwind masks of the owned faces for the chunk (cp.async target)
     const uint2 *cls_src;                       // masks of chunk 0 of the tile's first owned face
     size_t cls_stride;                          // F * VPL: from one chunk's masks to the next
@@ -336,6 +338,14 @@ template <int VPL> __device__ __forceinline__ void stage_common(const F32Inst &I
         sm.gnbr[j] = I.gs_nbr[e0 + j];
         sm.ga[j] = make_float2(I.gs_ax[e0 + j], I.gs_ay[e0 + j]);
     }
+    constexpr int SEG = TileSmem<VPL>::SEG;
+    for (int s = threadIdx.x; s < nG; s += kT) {  // four-entry stencils decoded once per item
+        const int j = gp[s];
+        if (gp[s + 1] - gp[s] != 4) continue;
+        sm.g4o[s] = make_int4(I.gs_nbr[j] * SEG, I.gs_nbr[j + 1] * SEG, I.gs_nbr[j + 2] * SEG, I.gs_nbr[j + 3] * SEG);
+        sm.g4x[s] = make_float4(I.gs_ax[j], I.gs_ax[j + 1], I.gs_ax[j + 2], I.gs_ax[j + 3]);
+        sm.g4y[s] = make_float4(I.gs_ay[j], I.gs_ay[j + 1], I.gs_ay[j + 2], I.gs_ay[j + 3]);
+    }
     if (threadIdx.x == 0) {
         sm.nS = nS;
         sm.nG = nG;
@@ -383,7 +393,27 @@ template <int VPL> __device__ __forceinline__ void gradients(TileSmem<VPL> &sm, 
             g[v] = make_float4(0.f, 0.f, 0.f, 0.f);
             c[v] = phi[s * SEG + v * 32 + lane];
         }
-        if (gradient_on) {
+        if (gradient_on && sm.gptr[s + 1] - sm.gptr[s] == 4) {  // the same sums, entries in order
+            const int4 o = sm.g4o[s];
+            const float4 ax = sm.g4x[s], ay = sm.g4y[s];
+            const int oo[4] = {o.x, o.y, o.z, o.w};
+            const float aa[4][2] = {{ax.x, ay.x}, {ax.y, ay.y}, {ax.z, ay.z}, {ax.w, ay.w}};
+            float2 x[4][VPL];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int v = 0; v < VPL; ++v) x[q][v] = phi[oo[q] + lane + v * 32];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int v = 0; v < VPL; ++v) {
+                    const float dg = x[q][v].x - c[v].x, dh = x[q][v].y - c[v].y;
+                    g[v].x = fmaf(aa[q][0], dg, g[v].x);
+                    g[v].y = fmaf(aa[q][1], dg, g[v].y);
+                    g[v].z = fmaf(aa[q][0], dh, g[v].z);
+                    g[v].w = fmaf(aa[q][1], dh, g[v].w);
+                }
+        } else if (gradient_on) {
             const int j0 = sm.gptr[s], j1 = sm.gptr[s + 1];
             int j = j0;
             for (; j + 4 <= j1; j += 4) {  // four stencil entries: all loads, then the sums in entry order
