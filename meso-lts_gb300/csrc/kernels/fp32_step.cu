@@ -101,18 +101,22 @@ __device__ __forceinline__ float expm1_dev(float x) {
 //   g_M = g0 + dg_M,  dg_M = g0 expm1(E)
 //   g_S - g0 = dg_M + g_M (1 - Pr) (c.q) / (5 p R T) (c^2 / RT - 4)
 //   h_S - h0 = hm dg_M + dhm g0 + g_M (1 - Pr) (c.q) / (5 p) ((c^2 / RT - 2)(K + 1) - 2K)
-__device__ __forceinline__ float2 dshakhov(const EqP &e, float xx, float xy, float xi2, float g0, float k3,
-                                           float twoK) {
+// dshakhov_c takes the peculiar velocity c = xi - u (cx, cy, cc = |c|^2); dshakhov forms it.
+__device__ __forceinline__ float2 dshakhov_c(const EqP &e, float xx, float xy, float xi2, float g0, float cx, float cy,
+                                             float cc, float k3, float twoK) {
     const float E = fmaf(e.ea, xi2, fmaf(e.ebx, xx, fmaf(e.eby, xy, e.ec)));
     const float dgm = g0 * expm1_dev(E);
     const float gm = g0 + dgm;
-    const float cx = xx - e.ux, cy = xy - e.uy;
-    const float cc = fmaf(cx, cx, cy * cy);
     const float a = gm * fmaf(cx, e.qgx, cy * e.qgy);  // g_M (1 - Pr) (c.q) / (5 p R T)
     const float dg = fmaf(a, fmaf(cc, e.iRT, -4.0f), dgm);
     // (c^2 / RT - 2)(K + 1) - 2K = c^2 (K + 1) / RT - 2 (K + 1) - 2K
     const float dh = fmaf(a * e.RT, fmaf(cc, e.iRTk3, fmaf(-2.0f, k3, -twoK)), fmaf(e.hm, dgm, e.dhm * g0));
     return make_float2(dg, dh);
+}
+__device__ __forceinline__ float2 dshakhov(const EqP &e, float xx, float xy, float xi2, float g0, float k3,
+                                           float twoK) {
+    const float cx = xx - e.ux, cy = xy - e.uy;
+    return dshakhov_c(e, xx, xy, xi2, g0, cx, cy, fmaf(cx, cx, cy * cy), k3, twoK);
 }
 
 // EqP of (rho, u, T, q), from FP64 macros, given irho = 1 / rho and iRT = 1 / (R T): FP64 runs at
@@ -706,14 +710,14 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
                     const float gn = fmaf(k.cm, sn.x - old.x, old.x);
                     const float hn = fmaf(k.cm, sn.y - old.y, old.y);
                     // state n+1 with q at n (:682-687)
-                    const float cx = xx[v] - k.e1.ux, cy = xy[v] - k.e1.uy;
-                    const float2 s1 = dshakhov(k.e1, xx[v], xy[v], x2[v], g0[v], k3, twoK);
+                    const float cx = xx[v] - k.e1.ux, cy = xy[v] - k.e1.uy, cc = fmaf(cx, cx, cy * cy);
+                    const float2 s1 = dshakhov_c(k.e1, xx[v], xy[v], x2[v], g0[v], cx, cy, cc, k3, twoK);
                     // evolution (:689-690)
                     const float g = k.C * (gn + k.hdt_tau * s1.x + k.hdt_taun * (sn.x - gn) - k.dt_v * fg[v]);
                     const float h = k.C * (hn + k.hdt_tau * s1.y + k.hdt_taun * (sn.y - hn) - k.dt_v * fh[v]);
                     Sn[(size_t)(cs + cl) * NVp + p[v]] = make_float2(fmaf(k.Cs, s1.x - g, g), fmaf(k.Cs, s1.y - h, h));
                     // heat-flux partial (:692)
-                    const float hw = 0.5f * w[v] * fmaf(fmaf(cx, cx, cy * cy), g, h);
+                    const float hw = 0.5f * w[v] * fmaf(cc, g, h);
                     qv[0] = fmaf(hw, cx, qv[0]);
                     qv[1] = fmaf(hw, cy, qv[1]);
                 }
