@@ -14,21 +14,28 @@
 #include "mesh.h"
 
 #include <algorithm>
+#include <array>
+#include <cstdint>
 #include <fstream>
 #include <iomanip>
 #include <map>
 #include <sstream>
+#include <unordered_map>
 
 namespace MESO {
 
+// Whitespace-separated tokens (the tokens `std::istream >> std::string` yields in the "C" locale),
+// scanned directly: mesh files have one record per line and hundreds of thousands of tokens.
 StringList Utils::split(const String &s) {
-    std::istringstream iss(s);
     StringList out;
-    String tok;
-    while (iss >> tok) {
-        tok.erase(std::remove(tok.begin(), tok.end(), '\r'), tok.end());
-        tok.erase(std::remove(tok.begin(), tok.end(), '\n'), tok.end());
-        out.push_back(tok);
+    out.reserve(8);
+    const char *p = s.data(), *e = p + s.size();
+    auto ws = [](char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r'; };
+    while (p < e) {
+        while (p < e && ws(*p)) ++p;
+        const char *b = p;
+        while (p < e && !ws(*p)) ++p;
+        if (p > b) out.emplace_back(b, p);
     }
     return out;
 }
@@ -196,23 +203,19 @@ Vector face_normal(ObjectType t, const Vector &cell_pos, const Vector &face_pos,
 // Canonical cyclic node sequence of a face: start at the smallest node and
 // walk towards its smaller neighbour.  Two faces are the same face exactly
 // when these sequences are equal (the reference's string key, geom.cpp:133-162).
-List<ObjectId> face_key(const List<ObjectId> &nl) {
-    const int len = (int)nl.size();
+void face_key(const ObjectId *nl, int len, ObjectId *key) {
     int pos = 0, mn = nl[0];
     for (int i = 0; i < len; ++i)
         if (nl[i] < mn) { pos = i; mn = nl[i]; }
     int lp = pos == 0 ? len - 1 : pos - 1;
     int rp = pos == len - 1 ? 0 : pos + 1;
     bool dir = nl[rp] < nl[lp];
-    List<ObjectId> key;
-    key.reserve(len);
     for (int c = 0; c < len; ++c) {
-        key.push_back(nl[pos]);
+        key[c] = nl[pos];
         pos = dir ? pos + 1 : pos - 1;
         if (pos < 0) pos = len - 1;
         if (pos > len - 1) pos = 0;
     }
-    return key;
 }
 
 // Face shapes and local node lists per cell shape (object.cpp:18-34).
@@ -246,21 +249,40 @@ Cell::Cell(ObjectId i, ObjectType t, List<ObjectId> nodes) : geom_type(t), id(i)
     face_id.assign(Geom::face_num(t), -1);
 }
 
+// Canonical face key (at most four nodes) padded with -1, hashed for the face table.
+struct FaceKey4 {
+    std::array<ObjectId, 4> n;
+    bool operator==(const FaceKey4 &o) const { return n == o.n; }
+};
+struct FaceKey4Hash {
+    size_t operator()(const FaceKey4 &k) const {
+        uint64_t h = 1469598103934665603ull;
+        for (ObjectId v : k.n) h = (h ^ (uint64_t)(uint32_t)v) * 1099511628211ull;
+        return (size_t)h;
+    }
+};
+
 void Mesh::generate_face() {
-    std::map<List<ObjectId>, ObjectId> maps[3];  // edge, quad, tria faces
+    // edge, quad, tria faces; a face is found again exactly when its canonical key matches
+    std::unordered_map<FaceKey4, ObjectId, FaceKey4Hash> maps[3];
+    for (auto &m : maps) m.reserve(2 * cells.size() + 16);
+    faces.reserve(faces.size() + 3 * cells.size() + 16);
     for (auto &cell : cells) {
         const auto &fg = face_geoms(cell.geom_type);
         const auto &fn = face_nodes(cell.geom_type);
         for (int fi = 0; fi < Geom::face_num(cell.geom_type); ++fi) {
             ObjectType gt = fg[fi];
-            List<ObjectId> nl;
-            for (int k : fn[fi]) nl.push_back(cell.node_id.at(k));
+            const int len = (int)fn[fi].size();
+            ObjectId nl[4];
+            for (int q = 0; q < len; ++q) nl[q] = cell.node_id.at(fn[fi][q]);
             int which = gt == Geom::Edge ? 0 : (gt == Geom::Quad ? 1 : 2);
-            auto key = face_key(nl);
+            FaceKey4 key;
+            key.n.fill(-1);
+            face_key(nl, len, key.n.data());
             auto it = maps[which].find(key);
             if (it == maps[which].end()) {
                 int fid = (int)faces.size();
-                faces.emplace_back(fid, gt, nl);
+                faces.emplace_back(fid, gt, List<ObjectId>(nl, nl + len));
                 maps[which][key] = fid;
                 auto &f = faces.back();
                 f.cell_id = {cell.id, cell.id};
@@ -329,8 +351,9 @@ void Mesh::build_geom(double scale) {
     const int D = dimension();
     min_cell_size = -1.0;
     max_cell_magnitude = -1.0;
+    NodeList nl;  // reused: one allocation for all cells and faces
     for (auto &cell : cells) {
-        NodeList nl;
+        nl.clear();
         for (int it : cell.node_id) nl.push_back(nodes.at(it));
         cell.position = centroid(nl);
         cell.volume = cell_volume(cell.geom_type, nl);
@@ -344,7 +367,7 @@ void Mesh::build_geom(double scale) {
         else max_cell_magnitude = (mcm > max_cell_magnitude) ? mcm : max_cell_magnitude;
     }
     for (auto &f : faces) {
-        NodeList nl;
+        nl.clear();
         for (int it : f.node_id) {
             nl.push_back(nodes[it]);
             nodes[it].group_id = f.group_id;
