@@ -40,6 +40,8 @@ void DevArena::release() {
     for (void *p : ptrs) cudaFree(p);
     ptrs.clear();
     bytes = 0;
+    cur = nullptr;
+    left = 0;
 }
 
 void derive_kparams(const meso_params &p, int dim, meso::KParams &k) {

@@ -18,17 +18,35 @@
 
 namespace meso_host {
 
-// Tracks the device allocations of one context.
+// The device allocations of one context: small arrays are carved (256-byte aligned) out of 8 MiB
+// blocks and large ones get their own allocation, so a context costs a few cudaMalloc / cudaFree
+// calls rather than one per array (admission and retirement of served solves).  `bytes` counts
+// what the blocks and large arrays hold on the device.
 struct DevArena {
+    static constexpr size_t kBlock = (size_t)8 << 20, kAlign = 256;
     std::vector<void *> ptrs;
     size_t bytes = 0;
+    char *cur = nullptr;
+    size_t left = 0;
     template <class T> T *alloc(size_t n) {
         if (n == 0) n = 1;
+        const size_t want = (n * sizeof(T) + kAlign - 1) / kAlign * kAlign;
+        if (want > kBlock / 4) return static_cast<T *>(raw(want));
+        if (want > left) {
+            cur = static_cast<char *>(raw(kBlock));
+            left = kBlock;
+        }
+        T *r = reinterpret_cast<T *>(cur);
+        cur += want;
+        left -= want;
+        return r;
+    }
+    void *raw(size_t nbytes) {
         void *p = nullptr;
-        if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) throw std::bad_alloc();
+        if (cudaMalloc(&p, nbytes) != cudaSuccess) throw std::bad_alloc();
         ptrs.push_back(p);
-        bytes += n * sizeof(T);
-        return static_cast<T *>(p);
+        bytes += nbytes;
+        return p;
     }
     void release();
     ~DevArena() { release(); }
