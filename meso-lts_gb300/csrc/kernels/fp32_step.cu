@@ -1,51 +1,61 @@
 // FP32-storage Shakhov CDUGKS step (2-D), tiled and fused.
 //
-// Storage: g, h interleaved as float2, velocity-contiguous per cell
-// ([cell][NVp], NVp = NV rounded up to 32 VPL), two buffers (state n, n+1).
-// VPL (velocities per lane) is 2 for velocity sets of 256 and more, 1 below:
-// a chunk is 32 VPL velocities, lane l of a warp handles velocities
-// chunk*32*VPL + v*32 + l, v < VPL.
-// A step is ten launches, each over all instances of a batch, replayed as one
-// CUDA graph:
+// Storage: g - g0, h - h0 (deviations from a reference Maxwellian) interleaved
+// as float2, velocity-contiguous per cell ([cell][NVp], NVp = NV rounded up to
+// 32 VPL), two buffers (state n, n+1).  VPL (velocities per lane) is 2 for
+// velocity sets of 256 and more, 1 below: a chunk is 32 VPL velocities, lane l
+// of a warp handles velocities chunk*32*VPL + v*32 + l, v < VPL.  Velocity sets
+// up to NVp = 2048 are "small": their face kernels take 8 lanes per face and
+// their boundary faces a warp each.
+// A step is eleven launches (one more per face kernel when a batch mixes
+// small and large velocity sets), each over all instances of a batch,
+// replayed as one CUDA graph:
 //
-//   P1  k32_reconstruct  per (tile, velocity group) CTA: the tile and its
-//                        two-ring halo of one chunk of 32 VPL velocities
+//   P1  k32_reconstruct  per (tile, velocity group) CTA of 24 warps: the tile
+//                        and its two-ring halo of one chunk of 32 VPL velocities
 //                        double-buffered in shared memory (16-byte cp.async
-//                        copies by all threads), least-squares gradients of the
-//                        tile and 1-ring cells once per chunk, and the half-step
-//                        upwind reconstruction of each face the tile owns
+//                        copies by all threads) with the owned faces' upwind
+//                        masks, least-squares gradients of the tile and 1-ring
+//                        cells once per chunk, and the half-step upwind
+//                        reconstruction of each face the tile owns
 //                        (cdugks_shakhov.cpp:223-276) stored to HBM (fbar, or
 //                        bnd_in for boundary faces)
-//   FMa k32_face_moments one warp per face: 11 raw moments about a reference
-//                        velocity of the stored reconstruction (FP32 terms,
-//                        compensated, FP64 warp sum)
+//   FMa k32_face_moments a warp (large sets) or 8 lanes (small sets) per face:
+//                        11 raw moments about a reference velocity of the
+//                        stored reconstruction (FP32 terms, compensated; FP64 or
+//                        float-float cross-lane sums)
 //       k32_face_macros  one thread per face, FP64: face rho, u, T, tau, q
 //                        (cdugks_shakhov.cpp:341-349) and the moment fluxes of
 //                        the reconstruction, by exact algebra on the moments
-//   FMb k32_face_eqflux  one warp per interior face: discrete moment fluxes of
-//                        the face Shakhov equilibrium (FP32 terms, FP64 result),
-//                        and the face's flux value (n0.xi) A (blend of the
-//                        reconstruction and the equilibrium) stored in place
-//   BND k32_boundary     one block per boundary face: blend, diffuse-wall
-//                        balance, inlets / outlets, symmetry, slip
-//                        (cdugks_shakhov.cpp:364-607), moment fluxes, flux values
+//   FMb k32_face_eqflux  a warp (large sets) or 8 lanes (small sets) per
+//                        interior face: discrete moment fluxes of the face
+//                        Shakhov equilibrium, and the face's flux value
+//                        (n0.xi) A (blend of the reconstruction and the
+//                        equilibrium) stored in place
+//   BND k32_boundary     a block (large sets) or a warp (small sets) per
+//                        boundary face: blend, diffuse-wall balance, inlets /
+//                        outlets, symmetry, slip (cdugks_shakhov.cpp:364-607),
+//                        moment fluxes, flux values
 //   CM  k32_cell_macros  one thread per cell, FP64: flux moments from the face
 //                        fluxes, conservative update, tau, evolution constants
 //                        (cdugks_shakhov.cpp:636-668), NaN / T<0 monitor
-//   P2  k32_update       per (tile, group) CTA: the tile's cells and the flux
-//                        values of every face touching them, one chunk at a
-//                        time; per cell and velocity the signed sum of its faces'
-//                        flux values, evolution to f-bar-plus, heat-flux partials
-//                        (cdugks_shakhov.cpp:616-696)
+//   P2  k32_update       per (tile, group) CTA of 24 warps: the tile's cells and
+//                        the flux values of every face touching them, one chunk
+//                        at a time; per cell and velocity the signed sum of its
+//                        faces' flux values, evolution to f-bar-plus, heat-flux
+//                        partials (cdugks_shakhov.cpp:616-696)
 //   QR  k32_heat_flux    q = sum of the heat-flux partials (FP64); then the mask
-//                        repair and the end-of-step counter
+//                        repair, the end-of-step counter and the residual check
+//                        with the convergence counter (k32_residual)
 //
 // The state is read twice and written once per step; each face's values are
 // written once (reconstruction), read and rewritten once (flux value) and read
 // by the one or two tiles whose cells it bounds.  Upwind classification is
-// exact: n.xi is evaluated in FP32 and re-evaluated in FP64 in the reference's
-// order when it lies within a rounding margin of zero.  Per-face and per-cell
-// scalar work (pow, divisions) runs one thread per face / cell in FP64.
+// exact: static per-face masks record the class of every velocity from n.xi in
+// FP64 in the reference's order (k32_cls_setup).  Per-face and per-cell scalar
+// work runs one thread per face / cell in FP64, sharing reciprocals: FP64 runs
+// at a small fraction of the FP32 rate on this GPU, so the velocity loops and
+// the cross-lane sums stay in FP32 (compensated, float-float where needed).
 #include <cfloat>
 #include <cstddef>
 #include <climits>
