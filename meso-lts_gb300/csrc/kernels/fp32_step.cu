@@ -202,6 +202,14 @@ __device__ __forceinline__ void g0_fluxes(const F32Inst &I, double nx, double ny
     o[3] = nx * (G[6] + G[8]) + ny * (G[7] + G[9]) + I.hm0 * (nx * G[1] + ny * G[2]);
 }
 
+// Packed FP32 pairs (sm_100 and later): each is the two scalar operations, rounded alike, in one
+// instruction; the (g, h) pairs of the step map onto them.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+
 __device__ __forceinline__ void kahan(float &s, float &c, float v) {
     const float y = v - c;
     const float t = s + y;
@@ -295,7 +303,7 @@ struct OwnedFace {     // P1: one face owned by the tile
 template <int VPL> struct __align__(128) TileSmem {
     static constexpr int SEG = 32 * VPL;         // velocities of one slot in a chunk
     float2 phi[2][F32_MAX_SLOTS * SEG];         // double-buffered chunk of the tile + halo (cp.async target)
-    float4 G[F32_MAX_GSLOTS * SEG];             // gradients (g_x, g_y, h_x, h_y) of tile + 1-ring cells
+    float4 G[F32_MAX_GSLOTS * SEG];             // gradients (g_x, h_x, g_y, h_y) of tile + 1-ring cells
     float2 ga[F32_MAX_GENT];                    // gradient stencil coefficients
     int4 g4o[F32_MAX_GSLOTS];                   // slots with four stencil entries: neighbour offsets into phi
     float4 g4x[F32_MAX_GSLOTS], g4y[F32_MAX_GSLOTS];  // and their coefficients
@@ -394,17 +402,17 @@ __device__ __forceinline__ void next_chunk(const float2 *S, int NVp, int ch, int
 }
 
 // Gradients of the first nG slots from phi[buf].
+// Gradients of the first nG slots from phi[buf], stored as (dg/dx, dh/dx, dg/dy, dh/dy).
 template <int VPL> __device__ __forceinline__ void gradients(TileSmem<VPL> &sm, int buf, int gradient_on) {
     constexpr int SEG = TileSmem<VPL>::SEG;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nG = sm.nG;
     const float2 *phi = sm.phi[buf];
     for (int s = warp; s < nG; s += kRW) {
-        float4 g[VPL];
-        float2 c[VPL];
+        float2 gx[VPL], gy[VPL], c[VPL];  // (g, h) pairs
 #pragma unroll
         for (int v = 0; v < VPL; ++v) {
-            g[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+            gx[v] = gy[v] = make_float2(0.f, 0.f);
             c[v] = phi[s * SEG + v * 32 + lane];
         }
         if (gradient_on && sm.gptr[s + 1] - sm.gptr[s] == 4) {  // the same sums, entries in order
@@ -421,11 +429,9 @@ template <int VPL> __device__ __forceinline__ void gradients(TileSmem<VPL> &sm, 
             for (int q = 0; q < 4; ++q)
 #pragma unroll
                 for (int v = 0; v < VPL; ++v) {
-                    const float dg = x[q][v].x - c[v].x, dh = x[q][v].y - c[v].y;
-                    g[v].x = fmaf(aa[q][0], dg, g[v].x);
-                    g[v].y = fmaf(aa[q][1], dg, g[v].y);
-                    g[v].z = fmaf(aa[q][0], dh, g[v].z);
-                    g[v].w = fmaf(aa[q][1], dh, g[v].w);
+                    const float2 d = sub2(x[q][v], c[v]);
+                    gx[v] = fma2(f2(aa[q][0]), d, gx[v]);
+                    gy[v] = fma2(f2(aa[q][1]), d, gy[v]);
                 }
         } else if (gradient_on) {
             const int j0 = sm.gptr[s], j1 = sm.gptr[s + 1];
@@ -443,11 +449,9 @@ template <int VPL> __device__ __forceinline__ void gradients(TileSmem<VPL> &sm, 
                 for (int q = 0; q < 4; ++q)
 #pragma unroll
                     for (int v = 0; v < VPL; ++v) {
-                        const float dg = x[q][v].x - c[v].x, dh = x[q][v].y - c[v].y;
-                        g[v].x = fmaf(a[q].x, dg, g[v].x);
-                        g[v].y = fmaf(a[q].y, dg, g[v].y);
-                        g[v].z = fmaf(a[q].x, dh, g[v].z);
-                        g[v].w = fmaf(a[q].y, dh, g[v].w);
+                        const float2 d = sub2(x[q][v], c[v]);
+                        gx[v] = fma2(f2(a[q].x), d, gx[v]);
+                        gy[v] = fma2(f2(a[q].y), d, gy[v]);
                     }
             }
             for (; j < j1; ++j) {
@@ -455,17 +459,14 @@ template <int VPL> __device__ __forceinline__ void gradients(TileSmem<VPL> &sm, 
                 const float2 a = sm.ga[j];
 #pragma unroll
                 for (int v = 0; v < VPL; ++v) {
-                    const float2 x = phi[nb + v * 32];
-                    const float dg = x.x - c[v].x, dh = x.y - c[v].y;
-                    g[v].x = fmaf(a.x, dg, g[v].x);
-                    g[v].y = fmaf(a.y, dg, g[v].y);
-                    g[v].z = fmaf(a.x, dh, g[v].z);
-                    g[v].w = fmaf(a.y, dh, g[v].w);
+                    const float2 d = sub2(phi[nb + v * 32], c[v]);
+                    gx[v] = fma2(f2(a.x), d, gx[v]);
+                    gy[v] = fma2(f2(a.y), d, gy[v]);
                 }
             }
         }
 #pragma unroll
-        for (int v = 0; v < VPL; ++v) sm.G[s * SEG + v * 32 + lane] = g[v];
+        for (int v = 0; v < VPL; ++v) sm.G[s * SEG + v * 32 + lane] = make_float4(gx[v].x, gx[v].y, gy[v].x, gy[v].y);
     }
 }
 
@@ -475,9 +476,9 @@ __device__ __forceinline__ float2 recon(const TileSmem<VPL> &sm, int buf, int s,
     constexpr int SEG = TileSmem<VPL>::SEG;
     const int k = s * SEG + v * 32 + (threadIdx.x & 31);
     const float2 x = sm.phi[buf][k];
-    const float4 g = sm.G[k];
+    const float4 g = sm.G[k];  // (dg/dx, dh/dx, dg/dy, dh/dy)
     const float ax = d.x - hx, ay = d.y - hy;
-    return make_float2(fmaf(ax, g.x, fmaf(ay, g.y, x.x)), fmaf(ax, g.z, fmaf(ay, g.w, x.y)));
+    return fma2(f2(ax), make_float2(g.x, g.y), fma2(f2(ay), make_float2(g.z, g.w), x));
 }
 
 // The upwind side is selected per lane (slot and offset), so lanes of one warp that upwind from
@@ -681,9 +682,9 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
             for (int r = 0; r < RC; ++r) {
                 const int cl = warp + kUW * r;
                 if (cl >= nc) break;
-                float fg[VPL], fh[VPL];
+                float2 fl[VPL];  // (g, h) outward flux sums
 #pragma unroll
-                for (int v = 0; v < VPL; ++v) fg[v] = fh[v] = 0.f;
+                for (int v = 0; v < VPL; ++v) fl[v] = make_float2(0.f, 0.f);
                 const int e0 = sm.cf_off[cl], e1 = sm.cf_off[cl + 1];
                 if (e1 - e0 == 4) {  // outward flux of the cell (:616-629), the four faces in entry order
                     const int4 o = sm.c4o[cl];
@@ -693,8 +694,7 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
                     for (int v = 0; v < VPL; ++v) {
                         const float2 a = ff[o.x + v * 32], b = ff[o.y + v * 32], c = ff[o.z + v * 32],
                                      d = ff[o.w + v * 32];
-                        fg[v] = fmaf(g.w, d.x, fmaf(g.z, c.x, fmaf(g.y, b.x, fmaf(g.x, a.x, fg[v]))));
-                        fh[v] = fmaf(g.w, d.y, fmaf(g.z, c.y, fmaf(g.y, b.y, fmaf(g.x, a.y, fh[v]))));
+                        fl[v] = fma2(f2(g.w), d, fma2(f2(g.z), c, fma2(f2(g.y), b, fma2(f2(g.x), a, fl[v]))));
                     }
                 } else {
 #pragma unroll 4
@@ -703,11 +703,7 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
                         const float2 *ff = sm.fv[buf] + (t & 0x7f) * SEG + lane;
                         const float sgn = (t & 0x80) ? -1.f : 1.f;
 #pragma unroll
-                        for (int v = 0; v < VPL; ++v) {
-                            const float2 val = ff[v * 32];
-                            fg[v] = fmaf(sgn, val.x, fg[v]);
-                            fh[v] = fmaf(sgn, val.y, fh[v]);
-                        }
+                        for (int v = 0; v < VPL; ++v) fl[v] = fma2(f2(sgn), ff[v * 32], fl[v]);
                     }
                 }
                 const CellK k = sm.ck[cl];
@@ -717,17 +713,18 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
                     const float2 old = sm.phi[buf][cl * SEG + v * 32 + lane];
                     // state n (cdugks_shakhov.cpp:673-680)
                     const float2 sn = dshakhov(k.en, xx[v], xy[v], x2[v], g0[v], k3, twoK);
-                    const float gn = fmaf(k.cm, sn.x - old.x, old.x);
-                    const float hn = fmaf(k.cm, sn.y - old.y, old.y);
+                    const float2 gn = fma2(f2(k.cm), sub2(sn, old), old);
                     // state n+1 with q at n (:682-687)
                     const float cx = xx[v] - k.e1.ux, cy = xy[v] - k.e1.uy, cc = fmaf(cx, cx, cy * cy);
                     const float2 s1 = dshakhov_c(k.e1, xx[v], xy[v], x2[v], g0[v], cx, cy, cc, k3, twoK);
-                    // evolution (:689-690)
-                    const float g = k.C * (gn + k.hdt_tau * s1.x + k.hdt_taun * (sn.x - gn) - k.dt_v * fg[v]);
-                    const float h = k.C * (hn + k.hdt_tau * s1.y + k.hdt_taun * (sn.y - hn) - k.dt_v * fh[v]);
-                    Sn[(size_t)(cs + cl) * NVp + p[v]] = make_float2(fmaf(k.Cs, s1.x - g, g), fmaf(k.Cs, s1.y - h, h));
+                    // evolution (:689-690): C (g^n + dt/2 g_S / tau + dt/2 (g_S^n - g^n) / tau^n - dt/V flux)
+                    float2 e = fma2(f2(k.hdt_tau), s1, gn);
+                    e = fma2(f2(k.hdt_taun), sub2(sn, gn), e);
+                    e = fma2(f2(-k.dt_v), fl[v], e);
+                    const float2 gh = mul2(f2(k.C), e);
+                    Sn[(size_t)(cs + cl) * NVp + p[v]] = fma2(f2(k.Cs), sub2(s1, gh), gh);
                     // heat-flux partial (:692)
-                    const float hw = 0.5f * w[v] * fmaf(cc, g, h);
+                    const float hw = 0.5f * w[v] * fmaf(cc, gh.x, gh.y);
                     qv[0] = fmaf(hw, cx, qv[0]);
                     qv[1] = fmaf(hw, cy, qv[1]);
                 }
@@ -996,7 +993,7 @@ __device__ __forceinline__ void eqflux_block(const FaceK &k, float2 n, float are
         const float2 gs = dshakhov(k.e, xx, xy, x2, t.w, k3, twoK);
         const float2 gb = gv[i];
         const float d = fmaf(n.x, xx, n.y * xy), knA = d * area;
-        fb[p] = make_float2(knA * fmaf(k.oCs, gb.x, k.Cs * gs.x), knA * fmaf(k.oCs, gb.y, k.Cs * gs.y));
+        fb[p] = mul2(f2(knA), fma2(f2(k.oCs), gb, mul2(f2(k.Cs), gs)));
         const float wkn = w * d;
         const float a = wkn * gs.x;
         b[0] += a;
