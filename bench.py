@@ -417,6 +417,7 @@ def run_served(tmp: str, count: int = 200, rate: float = 20.0, max_step: int = 8
             done[t] = (st.step, st.converged, st.run_state, sec[0], sec[1])
             srv.release(t)
     wall = time.perf_counter() - t0
+    gpu_ms, poll_ms, batch_steps = srv.stats()
     srv.close()
     lat = sorted(v[3] for v in done.values())
     steps = [v[0] for v in done.values()]
@@ -440,7 +441,8 @@ def run_served(tmp: str, count: int = 200, rate: float = 20.0, max_step: int = 8
     return {"workload": f"{count} cavity solves, Poisson arrivals {rate}/s (seed 2), sides {{16,24,32}} quads, "
                         "log10 Kn ~ U(-2,0), DVS {hGH 28x28, NC 21x21}, lid ~ U(0.05,0.15), FP32 storage, "
                         f"run to L2-relative residual 1e-6 on U per 100 steps (max-step {max_step})",
-            "max_members": members, "solves_per_s": count / wall, "wall_seconds": wall, "p50_s": q(0.50), "p99_s": q(0.99),
+            "max_members": members, "solves_per_s": count / wall, "wall_seconds": wall,
+            "batch_steps": batch_steps, "gpu_seconds": gpu_ms * 1e-3, "poll_host_seconds": (poll_ms - gpu_ms) * 1e-3, "p50_s": q(0.50), "p99_s": q(0.99),
             "converged": conv, "reached_max_step_or_failed": count - conv, "mean_steps": float(np.mean(steps)),
             "serial_fp64_solves_per_s_est": count / serial_s if serial_s > 0 else None,
             "serial_fp64_note": "FP64 step time of each request class x the steps each solve took, summed"}

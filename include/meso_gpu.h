@@ -383,6 +383,10 @@ int meso_server_result(meso_server *server, int64_t tag, double *rho, double *u,
 int meso_server_release(meso_server *server, int64_t tag);
 /* Device bytes held by the admitted solves. */
 int64_t meso_server_device_bytes(meso_server *server);
+/* Totals since creation: device time of the batch steps (ms), wall time spent inside
+ * meso_server_poll (ms; the rest of it is admission, retirement and batch rebuilds on the host),
+ * and batch steps issued.  No counterpart in the reference. */
+int meso_server_stats(meso_server *server, double *gpu_ms, double *poll_ms, int64_t *batch_steps);
 
 /* ---- allocation-free entry point --------------------------------------- */
 

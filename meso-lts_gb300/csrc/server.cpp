@@ -77,6 +77,7 @@ struct meso_server {
     int64_t used = 0;
     double last_ms = 0.0;
     int64_t steps_issued = 0;
+    double gpu_ms = 0.0, poll_ms = 0.0;  // device time of the batch steps / wall time inside polls
 };
 
 namespace {
@@ -217,6 +218,12 @@ int meso_server_submit(meso_server *s, const char *case_file, const meso_params 
 int meso_server_poll(meso_server *s, int32_t nsteps, int64_t *done_tags, int32_t max_done, int32_t *ndone) {
     if (!s) return fail(MESO_ERR_INVALID, "null server");
     if (ndone) *ndone = 0;
+    const auto t0 = Clock::now();
+    struct PollTimer {  // wall time of the poll, whichever way it returns
+        meso_server *s;
+        Clock::time_point t0;
+        ~PollTimer() { s->poll_ms += std::chrono::duration<double, std::milli>(Clock::now() - t0).count(); }
+    } timer{s, t0};
     if (cudaSetDevice(s->device) != cudaSuccess) return fail(MESO_ERR_CUDA, "cannot select the server's device");
     std::vector<int64_t> finished;
     int rc = retire(s, finished);  // solves that ended in the previous poll
@@ -241,6 +248,7 @@ int meso_server_poll(meso_server *s, int32_t nsteps, int64_t *done_tags, int32_t
         int32_t nrun = 0;
         if ((rc = meso_batch_step(s->batch, n, &nrun))) return rc;
         s->last_ms = meso_batch_last_step_ms(s->batch);
+        s->gpu_ms += s->last_ms;
         s->steps_issued += n;
     }
     if ((rc = retire(s, finished))) return rc;
@@ -285,5 +293,13 @@ int meso_server_release(meso_server *s, int64_t tag) {
 }
 
 int64_t meso_server_device_bytes(meso_server *s) { return s ? s->used : 0; }
+
+int meso_server_stats(meso_server *s, double *gpu_ms, double *poll_ms, int64_t *batch_steps) {
+    if (!s) return fail(MESO_ERR_INVALID, "null server");
+    if (gpu_ms) *gpu_ms = s->gpu_ms;
+    if (poll_ms) *poll_ms = s->poll_ms;
+    if (batch_steps) *batch_steps = s->steps_issued;
+    return MESO_OK;
+}
 
 }  // extern "C"

@@ -126,6 +126,7 @@ _SIGS = {
     "meso_server_result": (C.c_int, [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, C.c_void_p, _dp]),
     "meso_server_release": (C.c_int, [C.c_void_p, C.c_int64]),
     "meso_server_device_bytes": (C.c_int64, [C.c_void_p]),
+    "meso_server_stats": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_int64)]),
     # device pointers are passed as integers (c_void_p)
     "meso_shakhov_moments_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p,
@@ -411,6 +412,12 @@ class Server:
         n = C.c_int32()
         _check(lib().meso_server_poll(self._h, nsteps, tags, max_done, C.byref(n)))
         return [tags[i] for i in range(n.value)]
+
+    def stats(self) -> tuple:
+        """(device ms of the batch steps, wall ms inside poll, batch steps issued) since creation."""
+        g, w, n = C.c_double(), C.c_double(), C.c_int64()
+        _check(lib().meso_server_stats(self._h, C.byref(g), C.byref(w), C.byref(n)))
+        return g.value, w.value, n.value
 
     def counts(self) -> tuple:
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
