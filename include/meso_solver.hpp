@@ -23,26 +23,64 @@
 #ifndef MESO_SOLVER_HPP
 #define MESO_SOLVER_HPP
 
+#include <fstream>
+#include <iomanip>
 #include <stdexcept>
 #include <string>
 #include <vector>
+
+#include <algorithm>
+#include <cstdio>
 
 #include "meso_gpu.h"
 
 namespace MESO {
 namespace GPU {
 
-// Vector and Field<T>: the parts of include/core/vector.h and include/mesh/object.h:42-75 the step
-// loop and output read.
+// Vector and Field<T>: the parts of include/core/vector.h and include/mesh/object.h:42-75 a caller
+// of the solver reads: len, flag, values, operator[], heft, set_zero and output (field.cpp:98-173).
 struct Vector {
     double x = 0.0, y = 0.0, z = 0.0;
+    double &operator[](int k) { return k == 0 ? x : (k == 1 ? y : z); }
+    double operator[](int k) const { return k == 0 ? x : (k == 1 ? y : z); }
 };
+
+enum { cell_field_flag, face_field_flag, node_field_flag };
 
 template <class T> struct Field {
     int len = 0;
+    int flag = cell_field_flag;
     std::vector<T> values;
     T &operator[](int i) { return values[(size_t)i]; }
     const T &operator[](int i) const { return values[(size_t)i]; }
+
+    // Component id (0 x, 1 y, 2 z) of a vector field as a scalar field.
+    Field<double> heft(int id) const {
+        Field<double> r;
+        r.len = len;
+        r.flag = flag;
+        r.values.resize(values.size());
+        for (size_t i = 0; i < values.size(); ++i) r.values[i] = values[i][id];
+        return r;
+    }
+    void set_zero() { std::fill(values.begin(), values.end(), T()); }
+    // One value (a vector as "x y z") per line, 18 significant digits; an unopenable file is
+    // skipped with a warning on stderr, as the reference logs one and returns.
+    void output(const std::string &file_name) const {
+        std::ofstream fp(file_name, std::ios::out | std::ios::trunc);
+        if (!fp.is_open()) {
+            std::fprintf(stderr, "Cannot open file: %s\n", file_name.c_str());
+            return;
+        }
+        for (const T &v : values) write(fp, v);
+    }
+
+private:
+    static void write(std::ofstream &fp, double v) { fp << std::setprecision(18) << v << std::endl; }
+    static void write(std::ofstream &fp, const Vector &v) {
+        fp << std::setprecision(18) << v.x << " " << std::setprecision(18) << v.y << " " << std::setprecision(18)
+           << v.z << std::endl;
+    }
 };
 
 class Solver {

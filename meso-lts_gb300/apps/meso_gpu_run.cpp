@@ -1,11 +1,13 @@
 // meso_gpu_run: the reference's per-solve loop (src/meso/exec.cpp:141-165) over the GPU solver.
 //
-//   meso_gpu_run <case-file> [fp64|fp32] [--dump <file>]
+//   meso_gpu_run <case-file> [fp64|fp32] [--dump <file>] [--fields <prefix>]
 //
 // Runs initial(), output(), do_step() until max-step or run_state false (output() every
 // write-interval), output(), as the reference's meso-mpi does for one case file, with the
 // MESO::GPU::Solver drop-in (include/meso_solver.hpp).  --dump writes the final macroscopic fields
 // as raw doubles: ncell, step, solution_time, rho[ncell], u[3 ncell], T[ncell], q[3 ncell].
+// --fields writes them through the Field API as text: <prefix>rho.dat, <prefix>u.dat (the x
+// component, Field::heft(0)), <prefix>vel.dat (vectors).
 #include <cstdio>
 #include <cstring>
 #include <exception>
@@ -20,11 +22,12 @@ int main(int argc, char **argv) {
         return 2;
     }
     int precision = -1;
-    std::string dump;
+    std::string dump, fields;
     for (int i = 2; i < argc; ++i) {
         if (!std::strcmp(argv[i], "fp64")) precision = MESO_FP64;
         else if (!std::strcmp(argv[i], "fp32")) precision = MESO_FP32;
         else if (!std::strcmp(argv[i], "--dump") && i + 1 < argc) dump = argv[++i];
+        else if (!std::strcmp(argv[i], "--fields") && i + 1 < argc) fields = argv[++i];
     }
     try {
         MESO::GPU::Solver solver(argv[1], precision);
@@ -32,6 +35,11 @@ int main(int argc, char **argv) {
         solver.sync();
         std::printf("step %d  solution_time %.17g  run_state %d\n", solver.step, solver.solution_time,
                     solver.get_run_state() ? 1 : 0);
+        if (!fields.empty()) {
+            solver.rho_cell.output(fields + "rho.dat");
+            solver.vel_cell.heft(0).output(fields + "u.dat");
+            solver.vel_cell.output(fields + "vel.dat");
+        }
         if (!dump.empty()) {
             FILE *f = std::fopen(dump.c_str(), "wb");
             if (!f) throw std::runtime_error("cannot write " + dump);

@@ -31,7 +31,7 @@ def test_dropin_loop_matches_golden(gpu, tmp_path, name):
     d = tmp_path / name
     shutil.copytree(os.path.join(GOLDEN, "cases", name), d)
     out = tmp_path / "macros.bin"
-    r = _run(["case.txt", "fp64", "--dump", str(out)], str(d))
+    r = _run(["case.txt", "fp64", "--dump", str(out), "--fields", str(tmp_path / "f_")], str(d))
     assert r.returncode == 0, r.stderr
     raw = np.fromfile(out, dtype=np.float64)
     n, step = int(raw[0]), int(raw[1])
@@ -44,3 +44,7 @@ def test_dropin_loop_matches_golden(gpu, tmp_path, name):
         assert relerr(T, g["T"]) <= 1e-12 and relerr(q, g["q"]) <= 1e-12
     # output() wrote the reference's files (case-name directory, latest/ and step data)
     assert any(os.scandir(d)), "no output written"
+    # the Field API's text output (18 digits, a value or "x y z" per line) and heft
+    assert np.array_equal(np.loadtxt(tmp_path / "f_rho.dat"), rho)
+    assert np.array_equal(np.loadtxt(tmp_path / "f_u.dat"), u[:, 0])
+    assert np.array_equal(np.loadtxt(tmp_path / "f_vel.dat").reshape(n, 3), u)
