@@ -14,8 +14,8 @@
 //
 // MESO::GPU::Solver has the members that loop and output() use, with the reference's names and
 // meaning (include/solver/boltzmann/cdugks_shakhov.h:4-60, include/solver/solver.h:22-46): step,
-// solution_time, rho_cell, vel_cell, T_cell, q_cell, initial(), do_step(), output(),
-// get_run_state(), max_step(), write_interval().  One class serves the three solver kinds; the case
+// solution_time, rho_cell, vel_cell, T_cell, q_cell, mesh and dvs_mesh (read-only views),
+// initial(), do_step(), output(), get_run_state(), max_step(), write_interval().  One class serves the three solver kinds; the case
 // file's "solver" key picks the kind, as main.cpp:49-54 does.  Errors surface as the reference's
 // exceptions: std::invalid_argument for bad input, std::runtime_error otherwise.  The macroscopic
 // Fields are copied from the device when read through sync() (do_step() syncs at the residual
@@ -83,12 +83,38 @@ private:
     }
 };
 
+// Read-only views of the solver's mesh and velocity mesh (include/mesh/object.h:93-128,
+// include/mesh/mesh.h): the members a caller of the solver reads; the geometry itself lives in
+// the library.
+struct CellView {
+    int id = 0;
+    Vector position;
+    double volume = 0.0;
+    std::vector<int> face_id, neighbors;
+};
+struct FaceView {
+    int id = 0;
+    Vector position;
+    double area = 0.0;
+    int cell_id[2] = {-1, -1};
+    Vector normal_vector[2];
+};
+struct MeshView {
+    int NCELL = 0, NFACE = 0, NDFVL = 2;
+    double total_volume = 0.0, min_cell_size = 0.0;
+    std::vector<CellView> cells;
+    std::vector<FaceView> faces;
+    int dimension() const { return NDFVL; }
+};
+
 class Solver {
 public:
     int step = 0;
     double solution_time = 0.0;
     Field<double> rho_cell, T_cell;
     Field<Vector> vel_cell, q_cell;
+    MeshView mesh;      // physical mesh (original Gambit order)
+    MeshView dvs_mesh;  // velocity mesh: cell position = xi, volume = weight
 
     // precision: MESO_FP64 (the parity form), MESO_FP32, or -1 for the case file's "gpu-precision"
     explicit Solver(const std::string &case_file, int precision = -1) {
@@ -96,8 +122,11 @@ public:
         check(meso_case_load(case_file.c_str(), &k));
         meso_mesh_desc m;
         int32_t rnp = 0, ol = 0, onp = 0;
+        meso_dvs_desc d;
         int rc = meso_case_mesh(k, &m);
+        if (rc == MESO_OK) rc = meso_case_dvs(k, &d);
         if (rc == MESO_OK) rc = meso_case_loop_settings(k, &max_step_, &write_interval_, &rnp, &ol, &onp);
+        if (rc == MESO_OK) views(m, d);
         meso_case_free(k);
         check(rc);
         ncell_ = m.ncell;
@@ -146,6 +175,43 @@ private:
         if (rc == MESO_OK) return;
         if (rc == MESO_ERR_INVALID || rc == MESO_ERR_IO) throw std::invalid_argument(meso_last_error());
         throw std::runtime_error(meso_last_error());
+    }
+    void views(const meso_mesh_desc &m, const meso_dvs_desc &d) {
+        mesh.NCELL = m.ncell;
+        mesh.NFACE = m.nface;
+        mesh.NDFVL = m.dim;
+        mesh.total_volume = m.total_volume;
+        mesh.min_cell_size = m.min_cell_size;
+        mesh.cells.resize((size_t)m.ncell);
+        for (int i = 0; i < m.ncell; ++i) {
+            CellView &c = mesh.cells[(size_t)i];
+            c.id = i;
+            c.position = {m.cell_pos[3 * i], m.cell_pos[3 * i + 1], m.cell_pos[3 * i + 2]};
+            c.volume = m.cell_vol[i];
+            c.face_id.assign(m.cell_face + m.cell_face_ptr[i], m.cell_face + m.cell_face_ptr[i + 1]);
+            c.neighbors.assign(m.cell_nbr + m.cell_nbr_ptr[i], m.cell_nbr + m.cell_nbr_ptr[i + 1]);
+        }
+        mesh.faces.resize((size_t)m.nface);
+        for (int f = 0; f < m.nface; ++f) {
+            FaceView &v = mesh.faces[(size_t)f];
+            v.id = f;
+            v.position = {m.face_pos[3 * f], m.face_pos[3 * f + 1], m.face_pos[3 * f + 2]};
+            v.area = m.face_area[f];
+            v.cell_id[0] = m.face_cell[2 * f];
+            v.cell_id[1] = m.face_cell[2 * f + 1];
+            v.normal_vector[0] = {m.face_normal[3 * f], m.face_normal[3 * f + 1], m.face_normal[3 * f + 2]};
+            v.normal_vector[1] = {-v.normal_vector[0].x, -v.normal_vector[0].y, -v.normal_vector[0].z};
+        }
+        dvs_mesh.NCELL = d.nv;
+        dvs_mesh.NDFVL = m.dim;
+        dvs_mesh.cells.resize((size_t)d.nv);
+        for (int p = 0; p < d.nv; ++p) {
+            CellView &c = dvs_mesh.cells[(size_t)p];
+            c.id = p;
+            c.position = {d.xi[3 * p], d.xi[3 * p + 1], d.xi[3 * p + 2]};
+            c.volume = d.w[p];
+            dvs_mesh.total_volume += d.w[p];
+        }
     }
     void resize() {
         rho_cell.len = T_cell.len = vel_cell.len = q_cell.len = ncell_;

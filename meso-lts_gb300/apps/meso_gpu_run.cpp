@@ -35,6 +35,11 @@ int main(int argc, char **argv) {
         solver.sync();
         std::printf("step %d  solution_time %.17g  run_state %d\n", solver.step, solver.solution_time,
                     solver.get_run_state() ? 1 : 0);
+        double mass = 0.0, wsum = 0.0;
+        for (const auto &c : solver.mesh.cells) mass += solver.rho_cell[c.id] * c.volume;
+        for (const auto &c : solver.dvs_mesh.cells) wsum += c.volume;
+        std::printf("cells %d  faces %d  velocities %d  mass %.17g  weights %.17g\n", solver.mesh.NCELL,
+                    solver.mesh.NFACE, solver.dvs_mesh.NCELL, mass, wsum);
         if (!fields.empty()) {
             solver.rho_cell.output(fields + "rho.dat");
             solver.vel_cell.heft(0).output(fields + "u.dat");

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 import build
+import meso_gpu as mg
 from conftest import GOLDEN
 from helpers import relerr
 
@@ -44,6 +45,12 @@ def test_dropin_loop_matches_golden(gpu, tmp_path, name):
         assert relerr(T, g["T"]) <= 1e-12 and relerr(q, g["q"]) <= 1e-12
     # output() wrote the reference's files (case-name directory, latest/ and step data)
     assert any(os.scandir(d)), "no output written"
+    # the solver's mesh and velocity-mesh views
+    line = [l for l in r.stdout.splitlines() if l.startswith("cells ")][0].split()
+    c = mg.Case(str(d / "case.txt"))
+    assert int(line[1]) == c.ncell == n and int(line[5]) == c.nv
+    vol = c.arrays()["cell_vol"]
+    assert abs(float(line[7]) - float(np.sum(rho * vol))) <= 1e-12 * float(np.sum(rho * vol))
     # the Field API's text output (18 digits, a value or "x y z" per line) and heft
     assert np.array_equal(np.loadtxt(tmp_path / "f_rho.dat"), rho)
     assert np.array_equal(np.loadtxt(tmp_path / "f_u.dat"), u[:, 0])
