@@ -24,6 +24,7 @@
 #define MESO_SOLVER_HPP
 
 #include <fstream>
+#include <functional>
 #include <iomanip>
 #include <stdexcept>
 #include <string>
@@ -38,11 +39,36 @@ namespace MESO {
 namespace GPU {
 
 // Vector and Field<T>: the parts of include/core/vector.h and include/mesh/object.h:42-75 a caller
-// of the solver reads: len, flag, values, operator[], heft, set_zero and output (field.cpp:98-173).
+// of the solver reads: len, flag, values, operator[], get_mesh, MeshCellValueToField, heft,
+// set_zero and output (field.cpp:98-173).
 struct Vector {
     double x = 0.0, y = 0.0, z = 0.0;
     double &operator[](int k) { return k == 0 ? x : (k == 1 ? y : z); }
     double operator[](int k) const { return k == 0 ? x : (k == 1 ? y : z); }
+};
+
+// Read-only views of the solver's mesh and velocity mesh (include/mesh/object.h:93-128,
+// include/mesh/mesh.h): the members a caller of the solver reads; the geometry itself lives in
+// the library.
+struct CellView {
+    int id = 0;
+    Vector position;
+    double volume = 0.0;
+    std::vector<int> face_id, neighbors;
+};
+struct FaceView {
+    int id = 0;
+    Vector position;
+    double area = 0.0;
+    int cell_id[2] = {-1, -1};
+    Vector normal_vector[2];
+};
+struct MeshView {
+    int NCELL = 0, NFACE = 0, NDFVL = 2;
+    double total_volume = 0.0, min_cell_size = 0.0;
+    std::vector<CellView> cells;
+    std::vector<FaceView> faces;
+    int dimension() const { return NDFVL; }
 };
 
 enum { cell_field_flag, face_field_flag, node_field_flag };
@@ -51,8 +77,14 @@ template <class T> struct Field {
     int len = 0;
     int flag = cell_field_flag;
     std::vector<T> values;
+    const MeshView *mesh_ptr = nullptr;  // the solver's mesh (cell fields)
     T &operator[](int i) { return values[(size_t)i]; }
     const T &operator[](int i) const { return values[(size_t)i]; }
+    const MeshView *get_mesh() const { return mesh_ptr; }
+    // values[i] = func(cell i) over the mesh's cells
+    void MeshCellValueToField(const std::function<T(const CellView &)> &func) {
+        for (int i = 0; i < len; ++i) values[(size_t)i] = func(mesh_ptr->cells[(size_t)i]);
+    }
 
     // Component id (0 x, 1 y, 2 z) of a vector field as a scalar field.
     Field<double> heft(int id) const {
@@ -81,30 +113,6 @@ private:
         fp << std::setprecision(18) << v.x << " " << std::setprecision(18) << v.y << " " << std::setprecision(18)
            << v.z << std::endl;
     }
-};
-
-// Read-only views of the solver's mesh and velocity mesh (include/mesh/object.h:93-128,
-// include/mesh/mesh.h): the members a caller of the solver reads; the geometry itself lives in
-// the library.
-struct CellView {
-    int id = 0;
-    Vector position;
-    double volume = 0.0;
-    std::vector<int> face_id, neighbors;
-};
-struct FaceView {
-    int id = 0;
-    Vector position;
-    double area = 0.0;
-    int cell_id[2] = {-1, -1};
-    Vector normal_vector[2];
-};
-struct MeshView {
-    int NCELL = 0, NFACE = 0, NDFVL = 2;
-    double total_volume = 0.0, min_cell_size = 0.0;
-    std::vector<CellView> cells;
-    std::vector<FaceView> faces;
-    int dimension() const { return NDFVL; }
 };
 
 class Solver {
@@ -215,6 +223,8 @@ private:
     }
     void resize() {
         rho_cell.len = T_cell.len = vel_cell.len = q_cell.len = ncell_;
+        rho_cell.mesh_ptr = T_cell.mesh_ptr = &mesh;
+        vel_cell.mesh_ptr = q_cell.mesh_ptr = &mesh;
         rho_cell.values.assign((size_t)ncell_, 0.0);
         T_cell.values.assign((size_t)ncell_, 0.0);
         vel_cell.values.assign((size_t)ncell_, Vector());

@@ -36,7 +36,9 @@ int main(int argc, char **argv) {
         std::printf("step %d  solution_time %.17g  run_state %d\n", solver.step, solver.solution_time,
                     solver.get_run_state() ? 1 : 0);
         double mass = 0.0, wsum = 0.0;
-        for (const auto &c : solver.mesh.cells) mass += solver.rho_cell[c.id] * c.volume;
+        MESO::GPU::Field<double> m = solver.rho_cell;  // rho V per cell through the Field API
+        m.MeshCellValueToField([&](const MESO::GPU::CellView &c) { return solver.rho_cell[c.id] * c.volume; });
+        for (int i = 0; i < m.len; ++i) mass += m[i];
         for (const auto &c : solver.dvs_mesh.cells) wsum += c.volume;
         std::printf("cells %d  faces %d  velocities %d  mass %.17g  weights %.17g\n", solver.mesh.NCELL,
                     solver.mesh.NFACE, solver.dvs_mesh.NCELL, mass, wsum);
