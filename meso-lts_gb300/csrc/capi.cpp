@@ -506,7 +506,38 @@ bool capture_f32_graph(meso_ctx *c) {
     return true;
 }
 
+// The FP64 step's launches take the step constants (KParams) by value and fixed buffers, so they
+// are captured as a graph for the current constants and recaptured when a parameter change (live
+// reload, meso_set_params) alters them.
+bool capture_plain_graph(meso_ctx *c) {
+    if (c->plain_graph) cudaGraphExecDestroy(c->plain_graph);
+    c->plain_graph = nullptr;
+    cudaGraph_t g = nullptr;
+    int64_t n = 0;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+    const int rc = meso::plain_step(c->ps, c->stream, &n);
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    bool ok = rc == 0 && e == cudaSuccess && cudaGraphInstantiate(&c->plain_graph, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+        cudaGetLastError();
+        c->plain_graph = nullptr;
+        return false;
+    }
+    c->plain_graph_kp = c->ps.kp;
+    c->plain_graph_launches = n;
+    return true;
+}
+
 int launch_step(meso_ctx *c) {
+    if (c->params.precision != MESO_FP32 &&
+        ((c->plain_graph && std::memcmp(&c->plain_graph_kp, &c->ps.kp, sizeof(meso::KParams)) == 0) ||
+         capture_plain_graph(c))) {
+        if (cudaGraphLaunch(c->plain_graph, c->stream) != cudaSuccess)
+            return fail(MESO_ERR_CUDA, std::string("graph launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+        c->last_launches += c->plain_graph_launches;
+        return MESO_OK;
+    }
     if (c->params.precision == MESO_FP32 && (c->f32_graph_version == c->f32_version || capture_f32_graph(c))) {
         if (cudaGraphLaunch(c->f32_graph, c->stream) != cudaSuccess)
             return fail(MESO_ERR_CUDA, std::string("graph launch failed: ") + cudaGetErrorString(cudaGetLastError()));
@@ -859,6 +890,7 @@ void meso_ctx_destroy(meso_ctx *c) {
     cudaSetDevice(c->device);
     if (c->batch) meso_host::batch_forget(c->batch, c);
     if (c->f32_graph) cudaGraphExecDestroy(c->f32_graph);
+    if (c->plain_graph) cudaGraphExecDestroy(c->plain_graph);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->f32_fork.side) cudaStreamDestroy(c->f32_fork.side);
     if (c->f32_fork.fork) cudaEventDestroy(c->f32_fork.fork);

@@ -110,5 +110,8 @@ struct meso_ctx {
     meso::StepFork f32_fork;              // side stream and events of the captured step's branch
     int f32_graph_version = -1;
     int64_t f32_graph_launches = 0;
+    cudaGraphExec_t plain_graph = nullptr;  // the FP64 step's launches, captured for these kp
+    meso::KParams plain_graph_kp{};
+    int64_t plain_graph_launches = 0;
     meso_batch *batch = nullptr;  // the batch this context is a member of, if any
 };
