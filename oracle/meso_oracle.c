@@ -1,7 +1,7 @@
 /*
  * meso_oracle.c -- CPU restatement of the meso-lts step.  TEST INFRASTRUCTURE:
- * the checker for the GPU library and the timed CPU baseline; see
- * meso_oracle.h.  Every function cites the reference lines it restates
+ * the reference results the GPU library is tested against, and the timed CPU
+ * baseline; see meso_oracle.h.  Every function cites the reference lines it restates
  * (paths relative to the meso-lts project root).  Compile with
  * -ffp-contract=off: expressions are written in the reference's evaluation
  * order and must not be contracted into FMAs.

@@ -1,7 +1,8 @@
 /*
  * meso_oracle.h -- CPU restatement of the meso-lts step, TEST INFRASTRUCTURE.
  *
- * This library is the checker for the GPU step and the timed CPU baseline.
+ * This library gives the results the GPU step is tested against, and the timed
+ * CPU baseline.
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
  * load it; the product never does.
  *

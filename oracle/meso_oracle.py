@@ -2,7 +2,8 @@
 
 The CPU restatement of the meso-lts step (meso_oracle.c).  Only tests/,
 __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as the
-checker and the baseline; it is never part of the product path.
+results the GPU step is tested against and as the CPU baseline; it is never
+part of the product path.
 
 It takes the descriptor structs of a loaded case (anything exposing the
 ctypes attributes `mesh`, `dvs`, `marks_ptr`, `nmarks`, `params`, as
