@@ -161,7 +161,8 @@ typedef struct meso_params {
                                     (cdugks_shakhov.cpp:747-756), else MESO_RES_* bits; no counterpart
                                     in the reference (served solves converge on U) */
     /* FP32 kernel shape (0 = the library's choice or the autotuner's cached pick); no counterpart in
-       the reference: cells per tile (8..48), velocities per lane (1 or 2), velocity groups per tile */
+       the reference: cells per tile (8..48), velocities per lane (1 or 2), velocity groups per tile
+       (ngroup 0: the tiles' velocity chunks, tile after tile, cut into one equal run per SM) */
     int32_t tile_cells;
     int32_t vpl;
     int32_t ngroup;

@@ -36,13 +36,12 @@ std::vector<Shape> candidates(int nv, int ncell, int num_sms) {
     const int vmax = nv >= 64 ? 2 : 1;
     for (int T : {24, 32, 40, 48})
         for (int v = 1; v <= vmax; ++v) {
-            out.push_back({T, v, 0});
-            // more velocity groups when the mesh has few tiles for the SM count
+            out.push_back({T, v, 0});  // the tiles' velocity chunks in equal runs, one per SM
+            // equal velocity groups per tile instead, when the mesh has few tiles for the SM count
             const int tiles = (ncell + T - 1) / T;
             if (tiles < 2 * num_sms && nv >= 256) {
                 const int chunks = (nv + 32 * v - 1) / (32 * v);
-                const int ng = meso_host::default_ngroup(tiles, chunks, num_sms);
-                if (2 * ng <= chunks) out.push_back({T, v, 2 * ng});
+                out.push_back({T, v, meso_host::default_ngroup(tiles, chunks, num_sms)});
             }
         }
     return out;

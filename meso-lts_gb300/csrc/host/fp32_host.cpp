@@ -4,6 +4,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <queue>
+#include <utility>
 
 #include "capi_internal.h"
 
@@ -22,6 +25,73 @@ bool plan_fp32(const meso_mesh_desc &m, int tile_cells, Renumbering &rn, TilePla
             return true;
     }
     return false;
+}
+
+namespace {
+// A split over P runs: the first (ntile / P) P tiles go whole, tile t to run t % P, so that the
+// runs step through them in rounds of P neighbouring tiles, all at the same velocity chunk (the
+// halo cells one tile reads are read by its neighbours' CTAs at the same time, from L2).  The
+// chunks of the b = ntile % P tiles left, tile after tile, are cut into P equal runs of q (at
+// least two chunks where tiles have two), unless b is nearly P: then they go whole too.
+struct SplitShape {
+    int full, b;  // tiles of the whole rounds; tiles left
+    long q;       // chunks per run of the tiles left (0: they go whole)
+};
+SplitShape split_shape(int ntile, int chunks, int split) {
+    SplitShape sh;
+    sh.full = ntile / split * split;
+    sh.b = ntile - sh.full;
+    sh.q = 0;
+    if (sh.b > 0 && (long)sh.b * 10 < (long)split * 9)
+        sh.q = std::max(((long)sh.b * chunks + split - 1) / split, (long)std::min(2, chunks));
+    return sh;
+}
+}  // namespace
+
+std::vector<TilePiece> tile_pieces(int ntile, int chunks, int ngroup, int split) {
+    std::vector<TilePiece> out;
+    if (split <= 0) {  // ngroup groups of ceil(chunks / ngroup) chunks per tile
+        const int cpg = (chunks + ngroup - 1) / ngroup;
+        for (int t = 0; t < ntile; ++t)
+            for (int g = 0; g < ngroup; ++g) {
+                const int c0 = std::min(chunks, g * cpg), c1 = std::min(chunks, c0 + cpg);
+                out.push_back({t, g, c0, c1, -1});
+            }
+        return out;
+    }
+    const SplitShape sh = split_shape(ntile, chunks, split);
+    std::vector<int> cnt(ntile, 0);
+    auto whole = [&](int t, int r) {
+        out.push_back({t, 0, 0, chunks, r});
+        cnt[t] = 1;
+    };
+    for (int t = 0; t < sh.full; ++t) whole(t, t % split);
+    if (sh.q == 0) {
+        for (int t = sh.full; t < ntile; ++t) whole(t, t - sh.full);
+    } else {  // run r: chunks [r q, (r + 1) q) of the tiles left, cut at tile ends
+        const long total = (long)sh.b * chunks;
+        for (long r = 0; r * sh.q < total; ++r)
+            for (long a = r * sh.q, e = std::min(total, a + sh.q); a < e;) {
+                const int t = sh.full + (int)(a / chunks), c0 = (int)(a % chunks);
+                const int c1 = (int)std::min<long>(chunks, c0 + (e - a));
+                out.push_back({t, cnt[t]++, c0, c1, (int)r});
+                a += c1 - c0;
+            }
+    }
+    (void)ngroup;  // rows g >= cnt[t] of a tile are never written: zeroed once, when allocated
+    return out;
+}
+
+int split_ngroup(int ntile, int chunks, int split) {
+    const SplitShape sh = split_shape(ntile, chunks, split);
+    int most = 1;
+    if (sh.q == 0) return most;
+    // the pieces of left tile u are the runs that touch it: floor(u chunks / q) .. floor(((u + 1) chunks - 1) / q)
+    for (int u = 0; u < sh.b; ++u) {
+        const long r0 = (long)u * chunks / sh.q, r1 = ((long)(u + 1) * chunks - 1) / sh.q;
+        most = std::max(most, (int)(r1 - r0 + 1));
+    }
+    return most;
 }
 
 int default_ngroup(int ntile, int chunks, int num_sms) {
@@ -58,10 +128,15 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
     I.ntile = P.ntile;
     I.vpl = vpl;
     I.chunks = NVp / (32 * vpl);
-    I.ngroup = ngroup > 0 ? std::min(ngroup, I.chunks) : default_ngroup(P.ntile, I.chunks, c->num_sms);
-    {  // groups take ceil(chunks / ngroup) chunks each: drop groups that would be left empty
+    if (I.chunks > 0xffff) return fail(MESO_ERR_UNSUPPORTED, "FP32 form: more than 65535 velocity chunks");
+    if (ngroup > 0) {  // groups take ceil(chunks / ngroup) chunks each: drop groups that would be left empty
+        I.split = 0;
+        I.ngroup = std::min(ngroup, I.chunks);
         const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
         I.ngroup = (I.chunks + cpg - 1) / cpg;
+    } else {  // equal runs of chunks, one per SM
+        I.split = std::max(1, c->num_sms);
+        I.ngroup = split_ngroup(P.ntile, I.chunks, I.split);
     }
     const meso_params &p = c->params;
     I.dt = p.dt;
@@ -227,6 +302,8 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
         I.T_old = A.alloc<double>(C);
         I.q_old = A.alloc<double>(3 * (size_t)C);
         cudaMemsetAsync(I.resid, 0, sizeof(meso::F32Resid), s);
+        // heat-flux partial rows that no piece of a tile writes (a split tile's fewer groups) stay zero
+        cudaMemsetAsync(I.qpart, 0, sizeof(float4) * (size_t)I.ngroup * C, s);
         I.status = c->d_status;
         cudaMemsetAsync(I.S[0], 0, cv * sizeof(float2), s);
         cudaMemsetAsync(I.S[1], 0, cv * sizeof(float2), s);
@@ -256,26 +333,64 @@ int build_fp32_instance(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_des
 int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso::Fp32State &s,
                       std::vector<void *> &owned) {
     const int n = (int)insts.size();
-    std::vector<int2> items;
     std::vector<int> foff(1, 0), coff(1, 0), boff(1, 0);
     for (int i = 0; i < n; ++i) {
         const auto &I = insts[i];
-        for (int t = 0; t < I.ntile; ++t)
-            for (int g = 0; g < I.ngroup; ++g) items.push_back(make_int2(i, t * I.ngroup + g));
         foff.push_back(foff.back() + I.F);
         coff.push_back(coff.back() + I.C);
         boff.push_back(boff.back() + I.nb);
     }
-    // items of two-velocities-per-lane instances first (their own launch), then largest work first
-    // (persistent CTAs take items in order)
-    std::stable_sort(items.begin(), items.end(), [&](const int2 &a, const int2 &b) {
-        const auto &A = insts[a.x], &B = insts[b.x];
-        if (A.vpl != B.vpl) return A.vpl > B.vpl;
-        long wa = (long)((A.chunks + A.ngroup - 1) / A.ngroup), wb = (long)((B.chunks + B.ngroup - 1) / B.ngroup);
-        return wa > wb;
-    });
-    int n2 = 0;
-    for (const int2 &it : items) n2 += insts[it.x].vpl == 2 ? 1 : 0;
+    // Work items: the instances' tile pieces, one launch for instances with two velocities per
+    // lane and one for those with one.  A launch of a single split instance gives each CTA the
+    // pieces of its run; otherwise the pieces go, most chunks first, to the least-loaded CTA.  The
+    // results depend only on the pieces (each writes its own heat-flux partial row), not on the
+    // CTA that runs them.
+    std::vector<int4> items;
+    std::vector<int> off;
+    int grids[2] = {0, 0};
+    for (int k = 0; k < 2; ++k) {
+        const int vpl = 2 - k;
+        std::vector<std::pair<int, TilePiece>> ps;
+        int ninst_k = 0, only = -1;
+        for (int i = 0; i < n; ++i) {
+            const auto &I = insts[i];
+            if (I.vpl != vpl) continue;
+            ++ninst_k;
+            only = i;
+            for (const TilePiece &p : tile_pieces(I.ntile, I.chunks, I.ngroup, I.split)) ps.push_back({i, p});
+        }
+        std::vector<std::vector<int>> lists;
+        if (ninst_k == 1 && insts[only].split > 0 && insts[only].split <= num_sms) {
+            for (int j = 0; j < (int)ps.size(); ++j) {
+                const int r = ps[j].second.run;
+                if (r >= (int)lists.size()) lists.resize(r + 1);
+                lists[r].push_back(j);
+            }
+        } else if (!ps.empty()) {
+            std::vector<int> order(ps.size());
+            for (int j = 0; j < (int)ps.size(); ++j) order[j] = j;
+            auto cost = [&](int j) { return ps[j].second.ch1 - ps[j].second.ch0; };
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+            lists.resize(std::min((int)ps.size(), std::max(1, num_sms)));
+            std::priority_queue<std::pair<long, int>, std::vector<std::pair<long, int>>, std::greater<>> load;
+            for (int cta = 0; cta < (int)lists.size(); ++cta) load.push({0, cta});
+            for (int j : order) {
+                auto [l, cta] = load.top();
+                load.pop();
+                lists[cta].push_back(j);
+                load.push({l + cost(j), cta});
+            }
+        }
+        for (const auto &L : lists) {
+            off.push_back((int)items.size());
+            for (int j : L) {
+                const TilePiece &p = ps[j].second;
+                items.push_back(make_int4(ps[j].first, p.tile, p.grp, p.ch0 | (p.ch1 << 16)));
+            }
+        }
+        off.push_back((int)items.size());
+        grids[k] = (int)lists.size();
+    }
     // boundary faces: one block per face for large velocity sets, eight faces (a warp each) per
     // block for small ones
     std::vector<int2> bblocks, bblk;
@@ -298,18 +413,20 @@ int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso
         return p;
     };
     s.d_inst = (meso::F32Inst *)put(insts.data(), sizeof(meso::F32Inst) * n);
-    s.d_items = (int2 *)put(items.data(), sizeof(int2) * items.size());
+    s.d_items = (int4 *)put(items.data(), sizeof(int4) * items.size());
+    s.d_item_off = (int *)put(off.data(), sizeof(int) * off.size());
     s.d_face_items = (int *)put(foff.data(), sizeof(int) * foff.size());
     s.d_cell_items = (int *)put(coff.data(), sizeof(int) * coff.size());
     s.d_bnd_items = (int *)put(boff.data(), sizeof(int) * boff.size());
     s.d_bnd_blocks = (int2 *)put(bblocks.data(), sizeof(int2) * bblocks.size());
-    if (!s.d_inst || !s.d_items || !s.d_face_items || !s.d_cell_items || !s.d_bnd_items || !s.d_bnd_blocks)
+    if (!s.d_inst || !s.d_items || !s.d_item_off || !s.d_face_items || !s.d_cell_items || !s.d_bnd_items || !s.d_bnd_blocks)
         return -1;
     s.nbnd_blocks = (int)bblocks.size();
     s.nbnd_warp = nbw;
     s.ninst = n;
     s.nitems = (int)items.size();
-    s.nitems_vpl2 = n2;
+    s.grid2 = grids[0];
+    s.grid1 = grids[1];
     s.total_faces = foff.back();
     s.total_cells = coff.back();
     s.total_bnd = boff.back();

@@ -11,12 +11,6 @@ struct meso_ctx;
 
 namespace meso_host {
 
-// Tile size, velocity groups per tile: chosen by the autotuner or the defaults.
-struct Fp32Tuning {
-    int tile_cells = 64;
-    int ngroup = 0;  // 0: pick from the SM count
-};
-
 // Renumbering + tile plan that fits the kernel limits (shrinks the tile size until it does).
 bool plan_fp32(const meso_mesh_desc &m, int tile_cells, Renumbering &rn, TilePlan &plan);
 
@@ -30,5 +24,17 @@ int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso
 void free_fp32_launch(meso::Fp32State &s, std::vector<void *> &owned);
 
 int default_ngroup(int ntile, int chunks, int num_sms);
+
+// A piece of an instance's tile work: velocity chunks [ch0, ch1) of one tile, which write the
+// tile's heat-flux partial row `grp`; `run` is the CTA the piece was cut for (-1: any CTA).
+struct TilePiece {
+    int tile, grp, ch0, ch1, run;
+};
+// The pieces of an instance (F32Inst::split, ngroup): each tile's chunks once, in pieces that are
+// its groups 0, 1, ... (a split tile may have fewer than ngroup; its other partial rows are never
+// written and stay as zeroed when allocated).
+std::vector<TilePiece> tile_pieces(int ntile, int chunks, int ngroup, int split);
+// Groups per tile of a split over `split` runs (the largest number of pieces of one tile).
+int split_ngroup(int ntile, int chunks, int split);
 
 }  // namespace meso_host

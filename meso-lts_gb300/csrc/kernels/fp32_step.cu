@@ -11,7 +11,10 @@
 // small and large velocity sets), each over all instances of a batch,
 // replayed as one CUDA graph:
 //
-//   P1  k32_reconstruct  per (tile, velocity group) CTA of 24 warps: the tile
+//   P1  k32_reconstruct  persistent CTAs of 24 warps (one per SM) over their own
+//                        list of pieces (a tile and a range of its velocity
+//                        chunks; whole tiles in rounds of one per CTA, the
+//                        chunks of the tiles left cut into equal runs): the tile
 //                        and its two-ring halo of one chunk of 32 VPL velocities
 //                        double-buffered in shared memory (16-byte cp.async
 //                        copies by all threads) with the owned faces' upwind
@@ -39,11 +42,12 @@
 //   CM  k32_cell_macros  one thread per cell, FP64: flux moments from the face
 //                        fluxes, conservative update, tau, evolution constants
 //                        (cdugks_shakhov.cpp:636-668), NaN / T<0 monitor
-//   P2  k32_update       per (tile, group) CTA of 24 warps: the tile's cells and
+//   P2  k32_update       the same CTAs and pieces: the tile's cells and
 //                        the flux values of every face touching them, one chunk
 //                        at a time; per cell and velocity the signed sum of its
 //                        faces' flux values, evolution to f-bar-plus, heat-flux
-//                        partials (cdugks_shakhov.cpp:616-696)
+//                        partials, one row per piece of the tile
+//                        (cdugks_shakhov.cpp:616-696)
 //   QR  k32_heat_flux    q = sum of the heat-flux partials (FP64); then the mask
 //                        repair, the end-of-step counter and the residual check
 //                        with the convergence counter (k32_residual)
@@ -503,21 +507,20 @@ __device__ __forceinline__ float2 face_bar(const TileSmem<VPL> &sm, int buf, int
 // P1: upwind half-step reconstruction of every face (owned by a tile) into HBM
 // =============================================================================
 template <int VPL>
-__global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
-                                                    int nitems) {
+__global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restrict__ insts, const int4 *__restrict__ items,
+                                                    const int *__restrict__ item_off) {
     constexpr int SEG = TileSmem<VPL>::SEG;
     extern __shared__ float4 smem_raw[];
     TileSmem<VPL> &sm = *reinterpret_cast<TileSmem<VPL> *>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const int2 item = items[it];
+    for (int it = item_off[blockIdx.x]; it < item_off[blockIdx.x + 1]; ++it) {
+        const int4 item = items[it];  // (instance, tile, group, ch0 | ch1 << 16)
         const F32Inst &I = insts[item.x];
         if (step_stopped(I.status)) continue;
         const int cur = I.status->step & 1;  // S[step parity] holds the current state
-        const int tile = item.y / I.ngroup, grp = item.y % I.ngroup;
+        const int tile = item.y;
         const int fs = I.tile_fstart[tile], nOF = I.tile_fstart[tile + 1] - fs;
-        const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
-        const int ch0 = grp * cpg, ch1 = min(I.chunks, ch0 + cpg);
+        const int ch0 = item.w & 0xffff, ch1 = item.w >> 16;
         if (ch0 >= ch1) continue;
         const float2 *__restrict__ S = I.S[cur];
         const int NVp = I.NVp;
@@ -601,22 +604,21 @@ __device__ __forceinline__ void load_upd_chunk(const float2 *S, int NVp, int ch,
 }
 
 template <int VPL>
-__global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__ insts, const int2 *__restrict__ items,
-                                                   int nitems) {
+__global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__ insts, const int4 *__restrict__ items,
+                                                   const int *__restrict__ item_off) {
     constexpr int SEG = UpdSmem<VPL>::SEG;
     extern __shared__ float4 smem_raw[];
     UpdSmem<VPL> &sm = *reinterpret_cast<UpdSmem<VPL> *>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const int2 item = items[it];
+    for (int it = item_off[blockIdx.x]; it < item_off[blockIdx.x + 1]; ++it) {
+        const int4 item = items[it];  // (instance, tile, group, ch0 | ch1 << 16)
         const F32Inst &I = insts[item.x];
         if (step_stopped(I.status)) continue;
         const int cur = I.status->step & 1;  // S[step parity] holds the current state
-        const int tile = item.y / I.ngroup, grp = item.y % I.ngroup;
+        const int tile = item.y, grp = item.z;
         const int cs = I.tile_cstart[tile], nc = I.tile_ncell[tile];
-        const int cpg = (I.chunks + I.ngroup - 1) / I.ngroup;
-        const int ch0 = grp * cpg, ch1 = min(I.chunks, ch0 + cpg);
-        if (ch0 >= ch1) {  // an empty velocity group (not planned, see build_fp32_instance) adds nothing
+        const int ch0 = item.w & 0xffff, ch1 = item.w >> 16;
+        if (ch0 >= ch1) {  // a piece without chunks (a tile cut into fewer pieces than ngroup) adds nothing
             for (int c = threadIdx.x; c < nc; c += kUT) I.qpart[(size_t)grp * I.C + cs + c] = make_float4(0.f, 0.f, 0.f, 0.f);
             continue;
         }
@@ -1505,6 +1507,7 @@ __global__ void k32_heat_flux(const F32Inst *__restrict__ insts, const int *__re
         if (count_step && step_stopped(I.status)) continue;
         const int c = g - coff[i];
         double qx = 0.0, qy = 0.0;
+#pragma unroll 4
         for (int grp = 0; grp < I.ngroup; ++grp) {
             const float4 qp = I.qpart[(size_t)grp * I.C + c];
             qx += (double)qp.x + (double)qp.y;
@@ -1740,19 +1743,20 @@ const char *const kFp32Phases[] = {"k32_reconstruct", "k32_face_moments+macros",
 int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev, const StepFork *fork) {
     const int sms = s.num_sms;
     const int cap = sms * 32;
-    // one persistent CTA per SM; items of vpl == 2 instances, then those of vpl == 1, each its own launch
-    const int n2 = s.nitems_vpl2, n1 = s.nitems - s.nitems_vpl2;
-    const int grid2 = n2 < sms ? n2 : sms, grid1 = n1 < sms ? n1 : sms;
+    // persistent CTAs (at most one per SM) over their own item lists; items of vpl == 2 instances,
+    // then those of vpl == 1, each its own launch
+    const int grid2 = s.grid2, grid1 = s.grid1;
+    const int *off1 = s.d_item_off + grid2 + 1;
     int n = 0;
     auto tiles = [&](bool update) {
-        if (n2 > 0) {
-            if (update) k32_update<2><<<grid2, kUT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
-            else k32_reconstruct<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, n2);
+        if (grid2 > 0) {
+            if (update) k32_update<2><<<grid2, kUT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
+            else k32_reconstruct<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
             ++n;
         }
-        if (n1 > 0) {
-            if (update) k32_update<1><<<grid1, kUT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
-            else k32_reconstruct<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items + n2, n1);
+        if (grid1 > 0) {
+            if (update) k32_update<1><<<grid1, kUT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
+            else k32_reconstruct<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
             ++n;
         }
     };

@@ -69,6 +69,8 @@ struct CellK {
 struct F32Inst {
     int C, F, NV, NVp, nb, ntile, ngroup, chunks;  // chunks = NVp / (32 vpl)
     int vpl;                                       // velocities per lane: 1 or 2
+    int split;  // > 0: the tiles' velocity chunks, tile after tile, cut into `split` equal runs (one
+                // per persistent CTA); 0: each tile's chunks in ngroup equal groups
     // physics
     double dt, hdt, R, Pr, mu0, vhs, T0, Kd, Cv, gamma, rho0;
     float hdt32, k3_32, twoK32;  // FP32 copies of dt/2, K + 1 and 2K for the velocity loops
@@ -133,9 +135,11 @@ struct Fp32State {
     int enabled = 0;
     int ninst = 0;
     F32Inst *d_inst = nullptr;   // device copy of the instance array
-    int2 *d_items = nullptr;     // (inst, tile * ngroup + group) work items
+    int4 *d_items = nullptr;     // (inst, tile, group, ch0 | ch1 << 16) work items, grouped by CTA
+    int *d_item_off = nullptr;   // CTA c of the vpl == 2 launch runs items [off[c], off[c + 1]),
+                                 // CTA c of the vpl == 1 launch items [off[grid2 + 1 + c], ...)
     int nitems = 0;
-    int nitems_vpl2 = 0;         // the first nitems_vpl2 items belong to instances with vpl == 2
+    int grid2 = 0, grid1 = 0;    // CTAs of the two tile launches (instances with vpl 2 / 1)
     int *d_face_items = nullptr; // prefix sums of faces / cells / boundary faces over instances
     int *d_cell_items = nullptr;
     int *d_bnd_items = nullptr;
