@@ -163,6 +163,10 @@ int build_device(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d) {
     const int C = m->ncell, F = m->nface, NV = d->nv, D = m->dim;
     CUDA_TRY(cudaMallocHost(&c->h_mac, sizeof(double) * 8 * (size_t)C));
     const auto &rn = c->rn;
+    c->d_mac = c->arena.alloc<double>(8 * (size_t)C);
+    c->d_new2old = c->arena.alloc<int>(C);
+    CUDA_TRY(cudaMemcpyAsync(c->d_new2old, rn.cell_new2old.data(), sizeof(int) * (size_t)C, cudaMemcpyHostToDevice,
+                             c->stream));
     // ---- renumbered host tables
     std::vector<double> vol(C), cpos(3 * C), lsq_c(9 * C), lsq_w, lsq_dr, farea(F), fpos(3 * F), fn(3 * F);
     std::vector<int> cf_ptr(1, 0), cf_face, cn_ptr(1, 0), cn_cell, fown(F), fnei(F), fmark(F), bface;
@@ -342,26 +346,33 @@ int read_status(meso_ctx *c) {
 // contiguous device block into pinned staging, then the permutation.
 int fetch_macros(meso_ctx *c, double *rho, double *u, double *T, double *q) {
     const size_t C = (size_t)c->C;
-    double *h = c->h_mac;
-    if (c->ps.u == c->ps.rho + C && c->ps.T == c->ps.rho + 4 * C && c->ps.q == c->ps.rho + 5 * C) {
-        CUDA_TRY(cudaMemcpyAsync(h, c->ps.rho, sizeof(double) * 8 * C, cudaMemcpyDeviceToHost, c->stream));
-    } else {
-        CUDA_TRY(cudaMemcpyAsync(h, c->ps.rho, sizeof(double) * C, cudaMemcpyDeviceToHost, c->stream));
-        CUDA_TRY(cudaMemcpyAsync(h + C, c->ps.u, sizeof(double) * 3 * C, cudaMemcpyDeviceToHost, c->stream));
-        CUDA_TRY(cudaMemcpyAsync(h + 4 * C, c->ps.T, sizeof(double) * C, cudaMemcpyDeviceToHost, c->stream));
-        CUDA_TRY(cudaMemcpyAsync(h + 5 * C, c->ps.q, sizeof(double) * 3 * C, cudaMemcpyDeviceToHost, c->stream));
-    }
-    CUDA_TRY(cudaStreamSynchronize(c->stream));
-    const int *n2o = c->rn.cell_new2old.data();
-    for (size_t i = 0; i < C; ++i) {
-        const size_t o = (size_t)n2o[i];
-        if (rho) rho[o] = h[i];
-        if (T) T[o] = h[4 * C + i];
-        for (int k = 0; k < 3; ++k) {
-            if (u) u[3 * o + k] = h[C + 3 * i + k];
-            if (q) q[3 * o + k] = h[5 * C + 3 * i + k];
+    // permuted to the original cell order on the device, then one copy to the host; straight into
+    // the caller's arrays when all of them are page-locked
+    if (meso::gather_macros(c->ps.rho, c->ps.u, c->ps.T, c->ps.q, c->d_new2old, c->C, c->d_mac, c->num_sms, c->stream))
+        return fail(MESO_ERR_CUDA, "macro gather failed");
+    double *const dst[4] = {rho, u, T, q};
+    const size_t off[4] = {0, C, 4 * C, 5 * C}, len[4] = {C, 3 * C, C, 3 * C};
+    bool direct = true;
+    for (double *p : dst) {
+        if (!p) continue;
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost) {
+            cudaGetLastError();
+            direct = false;
         }
     }
+    if (direct) {
+        for (int k = 0; k < 4; ++k)
+            if (dst[k])
+                CUDA_TRY(cudaMemcpyAsync(dst[k], c->d_mac + off[k], sizeof(double) * len[k], cudaMemcpyDeviceToHost,
+                                         c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+        return MESO_OK;
+    }
+    CUDA_TRY(cudaMemcpyAsync(c->h_mac, c->d_mac, sizeof(double) * 8 * C, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < 4; ++k)
+        if (dst[k]) std::memcpy(dst[k], c->h_mac + off[k], sizeof(double) * len[k]);
     return MESO_OK;
 }
 

@@ -85,7 +85,9 @@ struct meso_ctx {
     meso::DMesh dm{};
     meso::DStatus *d_status = nullptr;
     meso::DStatus *h_status = nullptr;  // pinned mirror
-    double *h_mac = nullptr;            // pinned staging of the macros: rho, u (3), T, q (3) per cell
+    double *h_mac = nullptr;            // pinned staging of the macros: rho [C], u [3C], T [C], q [3C]
+    double *d_mac = nullptr;            // the same on the device, in original cell order (gather_macros)
+    int *d_new2old = nullptr;           // renumbered -> original cell index
     meso::PlainState ps{};
     meso::F32Inst f32{};               // FP32 instance (device pointers), when precision == MESO_FP32
     meso::Fp32State fs{};              // its single-instance launch state

@@ -1660,8 +1660,11 @@ __global__ void __launch_bounds__(512) k32_residual(const F32Inst *__restrict__ 
 }
 
 // =============================================================================
-// initial(): FP64 equilibrium per velocity, stored in FP32; FP64 moments
-// (cdugks_shakhov.cpp:81-168).  One warp per cell.
+// initial() (cdugks_shakhov.cpp:81-168), one warp per cell: the stored deviations are the cell's
+// equilibrium (mode 0: Maxwellian; mode 1: Shakhov with the given q) less the reference pair,
+// evaluated like every equilibrium of the step (dshakhov, FP32).  Mode 0 then sets the macros to
+// the discrete moments of the stored distribution: the reference pair's part in FP64 from its
+// discrete moments, the deviations' part as compensated FP32 lane sums, about the given velocity.
 // =============================================================================
 __global__ void k32_init(const F32Inst *__restrict__ insts, const int *__restrict__ coff, int ninst, int total,
                          int mode) {
@@ -1673,49 +1676,54 @@ __global__ void k32_init(const F32Inst *__restrict__ insts, const int *__restric
         const int c = g - coff[i];
         const int cur = I.status->step & 1;
         const double r = I.rho[c], ux = I.u[3 * c], uy = I.u[3 * c + 1], T = I.T[c];
-        const double qx = I.q[3 * c], qy = I.q[3 * c + 1];
-        const double RT = I.R * T, over = 0.5 / RT, p = r * RT;
-        double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const double qx = mode == 0 ? 0.0 : I.q[3 * c], qy = mode == 0 ? 0.0 : I.q[3 * c + 1];
+        const EqP e = make_eqp(I, r, ux, uy, T, qx, qy);
+        const float k3 = I.k3_32, twoK = I.twoK32, ux32 = (float)ux, uy32 = (float)uy;
+        float sm[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, cm[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float2 *__restrict__ S = I.S[cur] + (size_t)c * I.NVp;
         for (int pp = lane; pp < I.NVp; pp += 32) {
-            const double xx = I.xi64x[pp], xy = I.xi64y[pp], w = I.w64[pp];
-            const double cx = xx - ux, cy = xy - uy, cc = cx * cx + cy * cy;
-            const double gm = r * over / kPI * exp(-cc * over);
-            double gg, hh;
-            if (mode == 0) {
-                gg = gm;
-                hh = (I.Kd + 1.0) * RT * gm;
-            } else {
-                const double cq = cx * qx + cy * qy;
-                gg = (1.0 - I.Pr) * (cq / (5.0 * p * RT)) * (cc / RT - 4.0) * gm + gm;
-                hh = (1.0 - I.Pr) * (cq / (5.0 * p)) * ((cc / RT - 2.0) * (I.Kd + 1.0) - 2.0 * I.Kd) * gm +
-                     (I.Kd + 1.0) * RT * gm;
+            const float4 t = I.vt32[pp];  // xi_x, xi_y, w, g0
+            const float x2 = fmaf(t.x, t.x, t.y * t.y);
+            const float2 d = dshakhov(e, t.x, t.y, x2, t.w, k3, twoK);
+            S[pp] = d;
+            if (mode == 0) {  // w dg, w c dg, w (c^2 dg + dh), w c (c^2 dg + dh) about the given velocity
+                const float cx = t.x - ux32, cy = t.y - uy32, cc = fmaf(cx, cx, cy * cy);
+                const float wg = t.z * d.x, ws = t.z * fmaf(cc, d.x, d.y);
+                kahan(sm[0], cm[0], wg);
+                kahan(sm[1], cm[1], wg * cx);
+                kahan(sm[2], cm[2], wg * cy);
+                kahan(sm[3], cm[3], ws);
+                kahan(sm[4], cm[4], ws * cx);
+                kahan(sm[5], cm[5], ws * cy);
             }
-            const double g0 = I.g0_64[pp];
-            I.S[cur][(size_t)c * I.NVp + pp] = make_float2((float)(gg - g0), (float)(hh - I.hm0 * g0));
-            v[0] += w * gg;
-            v[1] += w * gg * xx;
-            v[2] += w * gg * xy;
-            v[3] += w * ((xx * xx + xy * xy) * gg + hh);
-            const double s = cc * gg + hh;
-            v[4] += w * cx * s;
-            v[5] += w * cy * s;
         }
-        for (int k = 0; k < 6; ++k)
-            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-        if (lane == 0) {
-            if (mode == 0) {
-                const double rho = v[0], vx = v[1] / rho, vy = v[2] / rho;
+        if (mode == 0) {
+            double v[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                v[k] = (double)sm[k] - (double)cm[k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+            }
+            if (lane == 0) {
+                double M0[F32_NMOM];  // the reference pair's moments about the given velocity
+                g0_raw_moments(I, ux, uy, M0);
+                const double rho = M0[0] + v[0];
+                const double mx = M0[1] + v[1], my = M0[2] + v[2];  // sum w c g
+                const double vx = ux + mx / rho, vy = uy + my / rho;
+                // sum w (xi^2 g + h) with xi = u + c
+                const double e2 = (M0[3] + M0[5] + M0[8] + v[3]) + 2.0 * (ux * mx + uy * my) + (ux * ux + uy * uy) * rho;
                 I.rho[c] = rho;
                 I.u[3 * c] = vx;
                 I.u[3 * c + 1] = vy;
                 I.u[3 * c + 2] = 0.0;
-                I.T[c] = (0.5 * v[3] / rho - 0.5 * (vx * vx + vy * vy)) / I.Cv;
-                I.q[3 * c] = 0.5 * v[4];
-                I.q[3 * c + 1] = 0.5 * v[5];
+                I.T[c] = (0.5 * e2 / rho - 0.5 * (vx * vx + vy * vy)) / I.Cv;
+                I.q[3 * c] = 0.5 * (M0[6] + M0[9] + v[4]);
+                I.q[3 * c + 1] = 0.5 * (M0[7] + M0[10] + v[5]);
                 I.q[3 * c + 2] = 0.0;
             }
-            I.u32[c] = make_float2((float)I.u[3 * c], (float)I.u[3 * c + 1]);
         }
+        if (lane == 0) I.u32[c] = make_float2((float)I.u[3 * c], (float)I.u[3 * c + 1]);
     }
 }
 

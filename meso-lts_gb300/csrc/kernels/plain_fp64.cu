@@ -899,6 +899,22 @@ __global__ void __launch_bounds__(kBlock) k_mask_repair(DMesh m, KParams k, DSta
     }
 }
 
+// Cell macros from the renumbered device arrays into one buffer in the caller's (original) cell
+// order: rho [C], u [3C], T [C], q [3C], so that one copy brings them to the host.
+__global__ void k_gather_macros(const double *__restrict__ rho, const double *__restrict__ u,
+                                const double *__restrict__ T, const double *__restrict__ q,
+                                const int *__restrict__ new2old, int C, double *__restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
+        const size_t o = (size_t)new2old[i], n = (size_t)C;
+        out[o] = rho[i];
+        out[4 * n + o] = T[i];
+        for (int k = 0; k < 3; ++k) {
+            out[n + 3 * o + k] = u[3 * (size_t)i + k];
+            out[5 * n + 3 * o + k] = q[3 * (size_t)i + k];
+        }
+    }
+}
+
 // End of step: count the step unless an earlier step stopped the run.
 __global__ void k_end_step(DStatus *st) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -1019,6 +1035,12 @@ int plain_step(const PlainState &s, cudaStream_t stream, int64_t *launches, cuda
 
 int plain_init(const PlainState &s, int mode, cudaStream_t stream) {
     return s.mesh.dim == 2 ? plain_init_dim<2>(s, mode, stream) : plain_init_dim<3>(s, mode, stream);
+}
+
+int gather_macros(const double *rho, const double *u, const double *T, const double *q, const int *new2old, int C,
+                  double *out, int sms, cudaStream_t stream) {
+    k_gather_macros<<<grid_for((size_t)C, sms), kBlock, 0, stream>>>(rho, u, T, q, new2old, C, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace meso

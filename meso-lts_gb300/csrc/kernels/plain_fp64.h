@@ -30,5 +30,9 @@ extern const char *const kPlainPhases[PLAIN_NPHASE];
 // One step; ev (may be null) receives PLAIN_NPHASE + 1 events around the phases.
 int plain_step(const PlainState &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev = nullptr);
 int plain_init(const PlainState &s, int mode, cudaStream_t stream);
+// rho [C], u [3C], T [C], q [3C] (renumbered, on the device) -> out [8C] in original cell order
+// (rho, u, T, q one after the other), out[new2old[i]] = rho[i] and so on.
+int gather_macros(const double *rho, const double *u, const double *T, const double *q, const int *new2old, int C,
+                  double *out, int sms, cudaStream_t stream);
 
 }  // namespace meso
