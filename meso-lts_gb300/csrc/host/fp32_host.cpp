@@ -399,7 +399,7 @@ int build_fp32_launch(const std::vector<meso::F32Inst> &insts, int num_sms, meso
         if (I.NVp <= meso::F32_SMALL_NVP) s.has_small = 1;
         else s.has_large = 1;
         if (I.NVp <= meso::F32_SMALL_NVP)
-            for (int b = 0; b < I.nb; b += 8) bblocks.push_back(make_int2(i, -b - 1));
+            for (int b = 0; b < I.nb; b += meso::F32_BND_FACES_PER_BLOCK) bblocks.push_back(make_int2(i, -b - 1));
         else
             for (int b = 0; b < I.nb; ++b) bblk.push_back(make_int2(i, b));
     }

@@ -210,7 +210,6 @@ __device__ __forceinline__ void g0_fluxes(const F32Inst &I, double nx, double ny
 // instruction; the (g, h) pairs of the step map onto them.
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 
@@ -1090,7 +1089,9 @@ __device__ __forceinline__ double solve_pressure(double P0, double R, double T, 
     return P0 / pow(1.0 + (gamma - 1.0) / 2.0 * (Ma * Ma), gamma / (gamma - 1.0));
 }
 
-constexpr int kBndThreads = 256;
+// Threads of a boundary block: one face (large velocity sets) or F32_BND_FACES_PER_BLOCK faces, a warp
+// each (small sets; the host plans the blocks' first faces with the same constant).
+constexpr int kBndThreads = 32 * F32_BND_FACES_PER_BLOCK;
 
 // Per-face scalars the group shares (written by its first warp).
 struct BndShared {
@@ -1352,11 +1353,9 @@ __global__ void __launch_bounds__(256) k32_bnd_setup(const F32Inst *__restrict__
         const F32Inst &I = insts[i];
         const int b = g - boff[i];
         const int f = I.bface[b];
-        const float2 n = I.fn32[f];
         const double2 n64 = I.fn64[f];
         double s0 = 0.0, s1 = 0.0;
         for (int p = threadIdx.x; p < I.NVp; p += blockDim.x) {
-            const float xx = I.xi32x[p], xy = I.xi32y[p];
             const int cls = cls_of(I, f, p);
             const double d = n64.x * I.xi64x[p] + n64.y * I.xi64y[p];
             const double t = d * I.w64[p] * I.g0_64[p];

@@ -130,6 +130,9 @@ struct F32Inst {
     double *rho_old, *u_old, *T_old, *q_old;  // macros at the last residual check
 };
 
+// Boundary faces of small velocity sets per boundary-kernel block (a warp each).
+constexpr int F32_BND_FACES_PER_BLOCK = 8;
+
 // Host-side handle of one or more instances sharing the phase launches.
 struct Fp32State {
     int enabled = 0;

@@ -44,8 +44,6 @@ static_assert(kCounterBytes % 256 == 0, "partials start on a 256-byte boundary")
 // cudaGetSymbolAddress, never a device address.
 static __device__ __align__(256) unsigned char g_moments_scratch[kScratchBytes];
 
-constexpr double kPI = 3.14159265358979323846;
-
 template <int DIM>
 __device__ __forceinline__ double dot3(double ax, double ay, double az, double bx, double by, double bz) {
     if (DIM == 2) return ax * bx + ay * by;
