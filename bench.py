@@ -24,6 +24,17 @@ Metric: cell-velocity updates per second (cells x velocities x steps / time).
 
 --impl reference times that CPU implementation alone (rank 0) on the same
 workload and prints the same JSON line with "impl": "reference".
+
+--profile WORKLOAD runs a few steps of one workload and prints the mean device
+time per step (and, with --phases, of each kernel phase), for profiler
+captures; no JSON line.  WORKLOAD: config1 (FP64 BGK cavity), config2 or
+config3 (--precision fp32|fp64), served64 (the first 64 requests of the served
+stream, stepped as one batch, one velocity group per tile as the server runs
+them).  A capture that collects more than gpu__time_duration.sum names one
+kernel, e.g.
+
+    ncu --set full --clock-control none -k regex:k32_update -s 2 -c 1 \
+        python bench.py --profile config2 --steps 3
 """
 from __future__ import annotations
 
@@ -448,6 +459,57 @@ def run_served(tmp: str, count: int = 200, rate: float = 20.0, max_step: int = 8
             "serial_fp64_note": "FP64 step time of each request class x the steps each solve took, summed"}
 
 
+def run_profile(args) -> int:
+    """A few steps of one workload for a profiler capture (no JSON line)."""
+    import cases
+    import meso_gpu as mg
+
+    with tempfile.TemporaryDirectory() as d:
+        if args.profile == "served64":
+            solvers, kases, work = [], [], 0
+            for r in cases.config5_requests(count=64):
+                case = mg.Case(cases.config5_case(os.path.join(d, f"s{r['index']}"), r, 8000))
+                rho, u, T, mask = case.initial_fields()
+                prm = case.params
+                prm.precision = mg.FP32
+                prm.ngroup = 1  # as the server runs requests that set no kernel shape
+                s = mg.Solver(case=case, precision=mg.FP32, mask=mask, params=prm)
+                s.init_macros(rho, u, T, None, 0)
+                solvers.append(s)
+                kases.append(case)
+                work += case.ncell * case.nv
+            b = mg.Batch(solvers)
+            b.step(args.steps)
+            ms = b.last_step_ms() / args.steps
+            print(f"served64: 64 solves, {work} cell-velocities, {ms:.3f} ms/step, "
+                  f"{work / ms * 1e3 / 1e9:.2f} G cell-xi/s")
+            if args.phases:
+                for k, v in b.phase_times(5).items():
+                    print(f"  {k}: {v:.4f} ms")
+            b.close()
+            for s in solvers:
+                s.close()
+            for case in kases:
+                case.close()
+            return 0
+        build = {"config1": lambda p: cases.config1(p, 10),
+                 "config2": lambda p: cases.config2(p, 10, args.precision),
+                 "config3": lambda p: cases.config3(p, 10, args.precision)}[args.profile]
+        case = mg.Case(build(os.path.join(d, args.profile)))
+        rho, u, T, mask = case.initial_fields()
+        prec = mg.FP32 if args.precision == "fp32" and args.profile != "config1" else mg.FP64
+        s = mg.Solver(case=case, precision=prec, mask=mask)
+        s.init_macros(rho, u, T, None, 0)
+        s.step(args.steps)
+        print(f"{args.profile} {'fp32' if prec == mg.FP32 else 'fp64'}: {case.ncell} cells x {case.nv} velocities, "
+              f"{s.last_step_ms() / args.steps:.3f} ms/step, {s.last_step_launches()} launches")
+        if args.phases:
+            for k, v in s.phase_times(5).items():
+                print(f"  {k}: {v:.4f} ms")
+        s.close()
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -459,7 +521,14 @@ def main() -> int:
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--served-count", type=int, default=200)
     ap.add_argument("--served-members", type=int, default=64, help="solves stepped together at most")
+    ap.add_argument("--profile", choices=["config1", "config2", "config3", "served64"],
+                    help="run a few steps of one workload for a profiler capture and exit")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="with --profile")
+    ap.add_argument("--phases", action="store_true", help="with --profile: per-phase device times")
     args = ap.parse_args()
+    if args.profile:
+        _cudart().cudaSetDevice(dist_env()[2])
+        return run_profile(args)
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
     dist = Dist(world)

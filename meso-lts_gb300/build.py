@@ -115,12 +115,15 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_LIB
 
 
-def build_reference() -> None:
-    """Builds oracle/_ref/meso_ref from the reference sources when they are present."""
-    script = os.path.join(ORACLE, "build_ref.sh")
-    src = os.environ.get("MESO_REF_SRC", "/root/reference")
-    if os.path.isdir(os.path.join(src, "src")) and shutil.which("g++"):
-        _run(["bash", script])
+def build_reference() -> bool:
+    """Builds oracle/_ref/meso_ref (test infrastructure) from a reference checkout named by the
+    MESO_REF_SRC environment variable; without it, or without the sources there, does nothing.
+    Not part of build_all(): the product build never reaches outside the repository."""
+    src = os.environ.get("MESO_REF_SRC")
+    if not src or not os.path.isdir(os.path.join(src, "src")) or not shutil.which("g++"):
+        return False
+    _run(["bash", os.path.join(ORACLE, "build_ref.sh")])
+    return True
 
 
 def build_all(force: bool = False) -> None:
@@ -130,7 +133,6 @@ def build_all(force: bool = False) -> None:
         a.result()
         b.result()
     build_apps(force)
-    build_reference()
 
 
 if __name__ == "__main__":

@@ -3,9 +3,11 @@
 #
 # Test infrastructure only: the binary is the reference itself, used to pin
 # the C restatement in oracle/ and to generate tests/golden/ fixtures.  It is
-# built from the sources where they lie (default /root/reference, or
-# $MESO_REF_SRC); nothing is copied into the repository.  Outputs go to
+# built from the sources where they lie, in the checkout that $MESO_REF_SRC
+# names (required); nothing is copied into the repository.  Outputs go to
 # oracle/_ref/ (git-ignored).
+#
+#   MESO_REF_SRC=<meso-lts checkout> bash oracle/build_ref.sh
 #
 # Substitutions, all project-written:
 #   * oracle/ref/mpi.h        single-rank MPI (the image has no MPI library)
@@ -18,7 +20,11 @@
 # Flags: -O2 -ffp-contract=off, so no FMA contraction on any host.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-SRC="${MESO_REF_SRC:-/root/reference}"
+if [ -z "${MESO_REF_SRC:-}" ]; then
+    echo "MESO_REF_SRC is not set: name the meso-lts checkout to build oracle/_ref from" >&2
+    exit 2
+fi
+SRC="$MESO_REF_SRC"
 OUT="$HERE/_ref"
 if [ ! -d "$SRC/src" ]; then
     echo "reference sources not found at $SRC; skipping oracle/_ref build" >&2
