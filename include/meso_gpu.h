@@ -226,6 +226,10 @@ int meso_case_initial_fields(const meso_case *c, double *rho, double *u, double 
 int meso_case_loop_settings(const meso_case *c, int32_t *max_step, int32_t *write_interval,
                             int32_t *read_np_data, int32_t *output_latest, int32_t *output_np);
 
+/* Mesh::output_grid (src/mesh/mesh_output.cpp:182-215): the case mesh's Tecplot grid file (the
+ * grid.plt output() writes at step 0), on the host; the zone header carries the node and cell counts. */
+int meso_case_output_grid(const meso_case *c, const char *path);
+
 /* ---- single solve ------------------------------------------------------- */
 
 /*
@@ -410,7 +414,10 @@ int meso_server_stats(meso_server *server, double *gpu_ms, double *poll_ms, int6
  *   rho [ncell], u [ncell*3], T [ncell], q [ncell*3]: outputs
  *   stream a cudaStream_t (NULL: the default stream); the outputs are ready
  *          when the stream reaches the call
- * Every array is device (or managed) memory of the current device.
+ * Every array is device (or managed) memory of the current device; a host
+ * pointer or another GPU's buffer fails with MESO_ERR_INVALID.  A CUDA error
+ * left pending by the caller's earlier work fails the call with
+ * MESO_ERR_CUDA and stays pending for the caller to read.
  *
  * Allocates nothing: no cudaMalloc, cudaFree or allocating library call.
  * Its scratch is one fixed device array of 8 MiB + 64 KiB in this library,

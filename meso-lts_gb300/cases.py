@@ -31,16 +31,17 @@ import numpy as np
 
 def _write_neu(path: str, nodes: np.ndarray, cells: list[list[int]], cell_type: int,
                bcs: dict[str, list[tuple[int, int, int]]], group: str = "fluid") -> None:
-    """nodes [N,2]; cells 0-based node lists; bcs name -> [(cell0, elemtype, face1based)]."""
+    """nodes [N,2] or [N,3]; cells 0-based node lists; bcs name -> [(cell0, elemtype, face1based)]."""
     n_nodes, n_cells = len(nodes), len(cells)
+    ndim = int(np.asarray(nodes).shape[1])
     with open(path, "w") as f:
         f.write("        CONTROL INFO 2.4.6\n** GAMBIT NEUTRAL FILE\nmeso-gb300 synthetic cavity\n")
         f.write("PROGRAM:  meso-gb300 cases.py     VERSION:  1.0\n01 Jan 2026 00:00:00\n")
         f.write("     NUMNP     NELEM     NGRPS    NBSETS     NDFCD     NDFVL\n")
-        f.write(f"{n_nodes:10d}{n_cells:10d}{1:10d}{len(bcs):10d}{2:10d}{2:10d}\nENDOFSECTION\n")
+        f.write(f"{n_nodes:10d}{n_cells:10d}{1:10d}{len(bcs):10d}{ndim:10d}{ndim:10d}\nENDOFSECTION\n")
         f.write("   NODAL COORDINATES 2.4.6\n")
-        for i, (x, y) in enumerate(nodes):
-            f.write(f"{i + 1:10d}{x:20.11E}{y:20.11E}\n")
+        for i, xyz in enumerate(nodes):
+            f.write(f"{i + 1:10d}" + "".join(f"{v:20.11E}" for v in xyz) + "\n")
         f.write("ENDOFSECTION\n      ELEMENTS/CELLS 2.4.6\n")
         for i, c in enumerate(cells):
             f.write(f"{i + 1:8d} {cell_type:2d} {len(c):2d} " + " ".join(f"{v + 1:8d}" for v in c) + "\n")
@@ -147,6 +148,80 @@ def jquad_cavity(path: str, n: int, seed: int = 0, jitter: float = 0.25) -> dict
                 wall.append((c, 2, 4))
     _write_neu(path, nodes, cells, 2, {"lid": lid, "wall": wall})
     return dict(ncell=n * n, min_cell_size=2.0 * math.sqrt(amin / math.pi))
+
+
+def brick_cavity(path: str, n: int, length: float = 1.0) -> dict:
+    """n^3 bricks on the unit cube (gambit element type 4, nodes in gambit order: x fastest, then y,
+    then z).  Local faces 1..6 = y-, x+, y+, x-, z-, z+ (object.cpp:32).  Marks: lid (y = 1, the moving
+    wall) and wall (the other five sides)."""
+    h = length / n
+    xs = np.arange(n + 1) * h
+    xs[-1] = length
+    Z, Y, X = np.meshgrid(xs, xs, xs, indexing="ij")
+    nodes = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    nid = lambda i, j, k: (k * (n + 1) + j) * (n + 1) + i
+    cells, lid, wall = [], [], []
+    for k in range(n):
+        for j in range(n):
+            for i in range(n):
+                c = len(cells)
+                cells.append([nid(i, j, k), nid(i + 1, j, k), nid(i, j + 1, k), nid(i + 1, j + 1, k),
+                              nid(i, j, k + 1), nid(i + 1, j, k + 1), nid(i, j + 1, k + 1), nid(i + 1, j + 1, k + 1)])
+                if j == n - 1:
+                    lid.append((c, 4, 3))
+                if j == 0:
+                    wall.append((c, 4, 1))
+                if i == n - 1:
+                    wall.append((c, 4, 2))
+                if i == 0:
+                    wall.append((c, 4, 4))
+                if k == 0:
+                    wall.append((c, 4, 5))
+                if k == n - 1:
+                    wall.append((c, 4, 6))
+    _write_neu(path, nodes, cells, 4, {"lid": lid, "wall": wall})
+    return dict(ncell=n ** 3, min_cell_size=2.0 * (3.0 * h ** 3 / (4.0 * math.pi)) ** (1.0 / 3.0))
+
+
+def tetra_cavity(path: str, n: int, length: float = 1.0) -> dict:
+    """n^3 cubes on the unit cube, each cut into six tetrahedra around its main diagonal (gambit element
+    type 6).  Local faces of a tetrahedron {1,0,2}, {0,1,3}, {1,2,3}, {2,0,3} (object.cpp:34).  Tetrahedra
+    with two faces on the boundary have two neighbours only (a singular 3x3 least-squares matrix,
+    geom.cpp:193-210), so cases on this mesh turn the gradient off.  Marks: lid (y = 1) and wall."""
+    h = length / n
+    xs = np.arange(n + 1) * h
+    xs[-1] = length
+    Z, Y, X = np.meshgrid(xs, xs, xs, indexing="ij")
+    nodes = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    nid = lambda i, j, k: (k * (n + 1) + j) * (n + 1) + i
+    faces_local = ((1, 0, 2), (0, 1, 3), (1, 2, 3), (2, 0, 3))
+    cells = []
+    for k in range(n):
+        for j in range(n):
+            for i in range(n):
+                v = lambda a, b, c: nid(i + a, j + b, k + c)
+                d0, d1 = v(0, 0, 0), v(1, 1, 1)
+                for path3 in ((v(1, 0, 0), v(1, 1, 0)), (v(1, 0, 0), v(1, 0, 1)), (v(0, 1, 0), v(1, 1, 0)),
+                              (v(0, 1, 0), v(0, 1, 1)), (v(0, 0, 1), v(1, 0, 1)), (v(0, 0, 1), v(0, 1, 1))):
+                    t = [d0, path3[0], path3[1], d1]
+                    a, b, c, d = (nodes[x] for x in t)
+                    if np.dot(np.cross(b - a, c - a), d - a) < 0.0:
+                        t = [t[0], t[2], t[1], t[3]]
+                    cells.append(t)
+    fmap = {}
+    for ci, t in enumerate(cells):
+        for fi, loc in enumerate(faces_local):
+            fmap.setdefault(tuple(sorted(t[x] for x in loc)), []).append((ci, fi))
+    lid, wall = [], []
+    for key, ents in fmap.items():
+        if len(ents) != 1:
+            continue
+        ci, fi = ents[0]
+        pts = nodes[list(key)]
+        (lid if np.all(pts[:, 1] == length) else wall).append((ci, 6, fi + 1))
+    _write_neu(path, nodes, cells, 6, {"lid": lid, "wall": wall})
+    vol = h ** 3 / 6.0
+    return dict(ncell=len(cells), min_cell_size=2.0 * (3.0 * vol / (4.0 * math.pi)) ** (1.0 / 3.0))
 
 
 def _tri_area(p, t):
@@ -546,6 +621,40 @@ def config5_case(d: str, req: dict, max_step: int = 4000) -> str:
     nv1d = {"d2q9": 3, "hgh": 28, "nc": 21}[req["dvs"]]
     return shakhov_cavity(d, "quad", req["side"], req["dvs"], nv1d, req["kn"], req["lid"], max_step,
                           name=f"req{req['index']}", precision="fp32", cfl=0.5)
+
+
+def shakhov_cavity3d(d: str, mesh: str = "brick", n: int = 4, nv1d: int = 9, kn: float = 0.5, lid: float = 0.15,
+                     steps: int = 20, cfl: float = 0.8, name: str = "cav3d", gradient: bool = True) -> str:
+    """3-D Shakhov cavity (brick or tetra mesh of n^3 cubes), Newton-Cotes nv1d^3 velocities on [-4, 4]^3
+    (the reference's 3-D Gauss-Hermite weights are wrong, dvs_generator.cpp:59,133; its Newton-Cotes set is
+    not), diffuse walls, lid moving along x."""
+    os.makedirs(d, exist_ok=True)
+    meshf = os.path.join(d, "mesh.neu")
+    info = brick_cavity(meshf, n) if mesh == "brick" else tetra_cavity(meshf, n)
+    newton_cotes(os.path.join(d, "v.dvs"), 1, nv1d - 1, 4.0)
+    dt = cfl * info["min_cell_size"] / (4.0 * math.sqrt(3.0))
+    settings = {"solver": "cdugks@shakhov", "case-name": name, "mesh-file": "mesh.neu", "dvs-file": "v.dvs",
+                "dvs-type": "Newton-Cotes", "write-interval": 1000, "max-step": steps, "Pr": 0.6666666666666667,
+                "gradient-switch": gradient, "limiter-switch": False, "output-np": False, "timeStep": dt,
+                "gas-constant": 0.5, "gas-k": 0, "ref-density": 1.0, "ref-length": 1.0, "ref-temperature": 1.0,
+                "ref-viscosity": viscosity_from_kn(kn), "vhs-index": 0.5}
+    marks = [{"name": "lid", "type": "wall", "velocity": _vec(lid), "temperature": _sc(1.0)},
+             {"name": "wall", "type": "wall", "velocity": _vec(0.0), "temperature": _sc(1.0)}]
+    return write_case(os.path.join(d, "case.txt"), settings,
+                      [{"name": "fluid", "density": _sc(1.0), "temperature": _sc(1.0)}], marks)
+
+
+def bgk_cavity3d(d: str, n: int = 4, steps: int = 40, lid: float = 0.1, name: str = "bgk3d") -> str:
+    """3-D incompressible BGK cavity on n^3 bricks with the 27-velocity Gauss-Hermite set (gh-3)."""
+    os.makedirs(d, exist_ok=True)
+    brick_cavity(os.path.join(d, "mesh.neu"), n)
+    gauss_hermite(os.path.join(d, "gh-3.dvs"), 3)
+    settings = {"solver": "cdugks@incompressible", "case-name": name, "mesh-file": "mesh.neu", "dvs-file": "gh-3.dvs",
+                "dvs-type": "Gauss-Hermite", "write-interval": 1000, "max-step": steps, "Re": 100.0,
+                "Ma": 0.1414213562373095, "gradient-switch": True, "timeStep": 2.5e-3, "gas-constant": 0.5,
+                "ref-density": 1.0, "ref-length": 1.0, "ref-temperature": 1.0}
+    return write_case(os.path.join(d, "case.txt"), settings, [{"name": "fluid", "density": _sc(1.0)}],
+                      [{"name": "lid", "type": "wall", "velocity": _vec(lid)}, {"name": "wall", "type": "wall"}])
 
 
 def shakhov_channel(d: str, kind: str = "pressure", nx: int = 10, ny: int = 6, dvs: str = "hgh", nv1d: int = 8,

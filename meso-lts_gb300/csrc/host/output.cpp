@@ -161,6 +161,8 @@ std::vector<double> comp(const std::vector<double> &v, int k) {
 
 }  // namespace
 
+void write_grid(const meso_case &k, const std::string &file) { output_grid(file, k.mesh); }
+
 void write_solver_output(const meso_case &k, int step, double t, const std::vector<double> &rho,
                          const std::vector<double> &u, const std::vector<double> &T, const std::vector<double> &q,
                          const std::vector<double> &m0, const std::vector<double> &m1, const std::vector<double> &m2) {

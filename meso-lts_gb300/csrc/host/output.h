@@ -1,6 +1,7 @@
 // Solver output in the reference's file formats.
 #pragma once
 
+#include <string>
 #include <vector>
 
 #include "case.h"
@@ -15,5 +16,8 @@ namespace meso_host {
 void write_solver_output(const meso_case &k, int step, double solution_time, const std::vector<double> &rho,
                          const std::vector<double> &u, const std::vector<double> &T, const std::vector<double> &q,
                          const std::vector<double> &m0, const std::vector<double> &m1, const std::vector<double> &m2);
+
+// Mesh::output_grid (mesh_output.cpp:182-215): the Tecplot grid file of the case's mesh.
+void write_grid(const meso_case &k, const std::string &file);
 
 }  // namespace meso_host

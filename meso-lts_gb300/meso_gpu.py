@@ -127,6 +127,7 @@ _SIGS = {
     "meso_server_release": (C.c_int, [C.c_void_p, C.c_int64]),
     "meso_server_device_bytes": (C.c_int64, [C.c_void_p]),
     "meso_server_stats": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_int64)]),
+    "meso_case_output_grid": (C.c_int, [C.c_void_p, C.c_char_p]),
     # device pointers are passed as integers (c_void_p)
     "meso_shakhov_moments_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p,
@@ -203,6 +204,10 @@ class Case:
         _check(lib().meso_case_loop_settings(self._h, *[C.byref(x) for x in v]))
         keys = ("max_step", "write_interval", "read_np_data", "output_latest", "output_np")
         return dict(zip(keys, (x.value for x in v)))
+
+    def output_grid(self, path: str) -> None:
+        """The mesh's Tecplot grid file (the grid.plt output() writes at step 0), on the host."""
+        _check(lib().meso_case_output_grid(self._h, os.fsencode(path)))
 
     def arrays(self) -> dict:
         """Copies of the flattened tables as numpy arrays (original order)."""

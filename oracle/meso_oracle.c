@@ -73,6 +73,8 @@ struct meso_oracle {
     double *rho_res, *T_res;
     V *u_res, *q_res;
     int step, run_state, converged, converge_state;
+    double last_res[8]; /* the last check's residual list, in the reference's print order */
+    int nres;
     double solution_time;
     Slice *slices;
     pthread_barrier_t bar;
@@ -846,6 +848,8 @@ static void after_step(meso_oracle *o) {
     }
     int conv = 1;
     for (int i = 0; i < n; ++i) conv = conv && (list[i] <= o->par.residual_limit);
+    for (int i = 0; i < n; ++i) o->last_res[i] = list[i];
+    o->nres = n;
     if (conv) o->converge_state++;
     else o->converge_state = 0;
     if (o->converge_state >= 10) {
@@ -1166,6 +1170,13 @@ int mo_get_state(const meso_oracle *o, int32_t *step, int32_t *run_state, int32_
     if (run_state) *run_state = o->run_state;
     if (converged) *converged = o->converged;
     if (t) *t = o->solution_time;
+    return MESO_OK;
+}
+
+int mo_get_residual(const meso_oracle *o, double *list, int32_t *n) {
+    if (!o || !list || !n) return MESO_ERR_INVALID;
+    for (int i = 0; i < o->nres; ++i) list[i] = o->last_res[i];
+    *n = o->nres;
     return MESO_OK;
 }
 

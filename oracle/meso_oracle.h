@@ -43,6 +43,9 @@ int mo_step(meso_oracle *o, int32_t nsteps, int32_t *steps_done);
 int mo_get_macros(const meso_oracle *o, double *rho, double *u, double *T, double *q);
 int mo_get_flux_moments(const meso_oracle *o, double *m0, double *m1, double *m2);
 int mo_get_state(const meso_oracle *o, int32_t *step, int32_t *run_state, int32_t *converged, double *solution_time);
+/* the last residual check's list (Res[Rho], Res[T], Res[u], ... in the reference's print order;
+ * cdugks_shakhov.cpp:729-746, cdugks.cpp:343-355) and its length (0 before the first check) */
+int mo_get_residual(const meso_oracle *o, double *list, int32_t *n);
 /* distribution of velocity p at cell c (d = 0: f or g, 1: h) */
 double mo_get_f(const meso_oracle *o, int32_t d, int32_t p, int32_t c);
 int mo_set_params(meso_oracle *o, const meso_params *params);

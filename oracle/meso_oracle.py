@@ -45,6 +45,8 @@ def lib() -> C.CDLL:
         L.mo_get_state.restype = C.c_int
         L.mo_get_f.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
         L.mo_get_f.restype = C.c_double
+        L.mo_get_residual.argtypes = [vp, dp, C.POINTER(C.c_int32)]
+        L.mo_get_residual.restype = C.c_int
         L.mo_set_params.argtypes = [vp, vp]
         L.mo_set_params.restype = C.c_int
         _lib = L
@@ -98,6 +100,13 @@ class Oracle:
         t = C.c_double()
         lib().mo_get_state(self._h, C.byref(s), C.byref(r), C.byref(c), C.byref(t))
         return dict(step=s.value, run_state=r.value, converged=c.value, solution_time=t.value)
+
+    def residual(self) -> np.ndarray:
+        """The last residual check's list, in the reference's print order."""
+        a = np.zeros(8)
+        n = C.c_int32()
+        lib().mo_get_residual(self._h, _p(a), C.byref(n))
+        return a[:n.value].copy()
 
     def f(self, d: int, p: int, c: int) -> float:
         return lib().mo_get_f(self._h, d, p, c)

@@ -7,7 +7,11 @@
 // then writes the macroscopic cell fields (and optionally the mesh/DVS tables
 // the solver built) as raw little-endian binary for the parity tests.
 //
-//   meso_ref <case-file> <nsteps> <out.bin> [--mesh <mesh.bin>] [--every K]
+//   meso_ref <case-file> <nsteps> <out.bin> [--mesh <mesh.bin>] [--every K] [--output 1]
+//
+// --output 1 calls the solver's own output() after initial() and after the
+// last step, as handle_solver does (exec.cpp:150-164): grid.plt, step-N/
+// data.plt and latest/ text files under the case-name folder.
 //
 // The case file's relative paths are resolved against the current directory,
 // exactly as the reference does; run it from the case directory.
@@ -101,10 +105,11 @@ void write_mesh(const std::string &path, MESO::fvmMesh::Mesh &m, MESO::fvmMesh::
 
 template <class S>
 int run(MESO::ArgParser &parser, MESO::Solver::Config &config, int nsteps, const std::string &out,
-        const std::string &mesh_out, int every) {
+        const std::string &mesh_out, int every, int output) {
     S s(parser, config);
     if (!mesh_out.empty()) write_mesh(mesh_out, s.mesh, s.dvs_mesh);
     s.initial();
+    if (output) s.output();
     auto t0 = std::chrono::steady_clock::now();
     for (int i = 0; i < nsteps; ++i) {
         s.do_step();
@@ -120,6 +125,7 @@ int run(MESO::ArgParser &parser, MESO::Solver::Config &config, int nsteps, const
         }
     }
     double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (output) s.output();
     Out o(out);
     if constexpr (std::is_same_v<S, MESO::Solver::CDUGKS_SHAKHOV>)
         write_macros(o, s, &s.T_cell, &s.q_cell, secs);
@@ -139,11 +145,12 @@ int main(int argc, char **argv) {
     int nsteps = std::atoi(argv[2]);
     std::string out = argv[3];
     std::string mesh_out;
-    int every = 0;
+    int every = 0, output = 0;
     for (int i = 4; i + 1 < argc; i += 2) {
         std::string k = argv[i];
         if (k == "--mesh") mesh_out = argv[i + 1];
         else if (k == "--every") every = std::atoi(argv[i + 1]);
+        else if (k == "--output") output = std::atoi(argv[i + 1]);
     }
     char a0[] = "meso_ref", a1[] = "--case";
     std::vector<char> a2(case_file.begin(), case_file.end());
@@ -158,11 +165,11 @@ int main(int argc, char **argv) {
     int rc = 3;
     try {
         if (solver == "dugks@incompressible")
-            rc = run<MESO::Solver::DUGKS>(parser, config, nsteps, out, mesh_out, every);
+            rc = run<MESO::Solver::DUGKS>(parser, config, nsteps, out, mesh_out, every, output);
         else if (solver == "cdugks@incompressible")
-            rc = run<MESO::Solver::CDUGKS>(parser, config, nsteps, out, mesh_out, every);
+            rc = run<MESO::Solver::CDUGKS>(parser, config, nsteps, out, mesh_out, every, output);
         else if (solver == "cdugks@shakhov")
-            rc = run<MESO::Solver::CDUGKS_SHAKHOV>(parser, config, nsteps, out, mesh_out, every);
+            rc = run<MESO::Solver::CDUGKS_SHAKHOV>(parser, config, nsteps, out, mesh_out, every, output);
         else
             std::fprintf(stderr, "unknown solver %s\n", solver.c_str());
     } catch (const std::exception &e) {

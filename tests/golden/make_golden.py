@@ -1,8 +1,11 @@
 """Generates tests/golden/: small case inputs and the reference's own outputs on them.
 
-Run here (where the reference sources and oracle/_ref/meso_ref exist):
+Run where the reference sources and oracle/_ref/meso_ref exist:
 
-    bash oracle/build_ref.sh && python tests/golden/make_golden.py
+    MESO_REF_SRC=<meso-lts checkout> bash oracle/build_ref.sh
+    MESO_REF_SRC=<meso-lts checkout> python tests/golden/make_golden.py [name ...]
+
+(no names: every case).
 
 For every case below it writes the inputs (case.txt, mesh.neu, the .dvs file)
 into tests/golden/cases/<name>/, runs the unmodified reference solver through
@@ -11,6 +14,20 @@ macroscopic fields (rho, u, T, q), step count, run_state and solution time in
 <name>.npz.  Two cases also store the mesh and DVS tables the reference built
 (geometry_<name>.npz).  The inputs are committed so the fixtures do not depend
 on the scipy / numpy versions that generated them.
+
+Further cases:
+  * ref_*: the reference's own shipped inputs (files/cavity.neu with
+    case-re400.txt, case-re1000.txt and case-kn0.075.txt and their velocity
+    sets; files/case-neumann.txt with its gambit physical and velocity
+    meshes), copied verbatim from the checkout MESO_REF_SRC names as test
+    inputs.
+  * *_blowup cases store the step at which the reference stops with a NaN /
+    T < 0 cell (run_state 0).
+  * OUTPUT cases also keep the reference's output() files (grid.plt,
+    step-N/data.plt or result-N, latest/*) under output/<name>/.
+  * RESTART cases run twice: the first run writes latest/ through output(),
+    the second starts from it with read-np-data True; the first run's latest/
+    files are kept as inputs of the second, whose fields are the golden.
 """
 from __future__ import annotations
 
@@ -46,6 +63,62 @@ GOLDEN = {
     "channel_farfield": (lambda d: cases.shakhov_channel(d, "farfield", steps=60), 60),
 }
 GEOMETRY = ("shakhov_m10_nc21", "channel_pressure")
+
+
+def _with_key(case_path: str, key: str, value: str) -> str:
+    _set_key(case_path, key, value)
+    return case_path
+
+
+def _ref_file(rel: str) -> str:
+    src = os.environ.get("MESO_REF_SRC")
+    if not src:
+        sys.exit("MESO_REF_SRC must name the reference checkout")
+    return os.path.join(src, "files", rel)
+
+
+def _ref_case(case_file: str, extra: list[str]):
+    """Copies one of the reference's shipped cases (and the files it reads) into d."""
+
+    def build(d):
+        os.makedirs(d, exist_ok=True)
+        for rel in [case_file] + extra:
+            dst = os.path.join(d, rel)
+            os.makedirs(os.path.dirname(dst), exist_ok=True)
+            shutil.copyfile(_ref_file(rel), dst)
+        return os.path.join(d, case_file)
+
+    return build
+
+
+GOLDEN.update({
+    # the reference's own inputs
+    "ref_re400": (_ref_case("case-re400.txt", ["cavity.neu", "gh-3.dvs"]), 300),
+    "ref_re1000": (_ref_case("case-re1000.txt", ["cavity.neu", "hGH.dvs"]), 40),
+    "ref_kn0075": (_ref_case("case-kn0.075.txt", ["cavity.neu", "nc.dvs"]), 5),
+    "ref_neumann": (_ref_case("case-neumann.txt", ["neumann/neumann_phy.neu", "neumann/neumann_dvs.neu"]), 4),
+    # where the reference scheme blows up: the transitional cavity (61x61 quads, hGH 28^2, Kn 0.075) at
+    # CFL 0.8, and the Delaunay-triangle cavity of the rarefied workload (7938 triangles, corner
+    # triangles flipped; NC 21^2 velocities, Kn 1, CFL 0.8)
+    "config3_cfl08_blowup": (lambda d: cases.shakhov_cavity(d, "quad", 61, "hgh", 28, 0.075, 0.15, 400,
+                                                            name="config3", cfl=0.8), 400),
+    "tri64_nc21_blowup": (lambda d: cases.shakhov_cavity(d, "tri", 64, "nc", 21, 1.0, 0.15, 200, name="tri64",
+                                                         cfl=0.8), 200),
+    # output() files and the read-np-data restart
+    "out_shakhov_q8": (lambda d: cases.shakhov_cavity(d, "quad", 8, "hgh", 8, 0.1, 0.15, 20, name="outs"), 20),
+    "out_cdugks_q8": (lambda d: cases.bgk_cavity(d, 8, 30, name="outb"), 30),
+    "restart_shakhov_q8": (lambda d: cases.shakhov_cavity(d, "quad", 8, "hgh", 8, 0.1, 0.15, 20, name="rs"), 20),
+    "restart_cdugks_q8": (lambda d: cases.bgk_cavity(d, 8, 30, name="rb"), 30),
+    # 3-D: bricks with the gradient, tetrahedra without (their corner cells have two neighbours);
+    # Newton-Cotes 9^3 velocities on [-4, 4]^3, W and qz in the output
+    "shakhov_brick4_nc9": (lambda d: cases.shakhov_cavity3d(d, "brick", 4, 9, 0.5, 0.15, 20), 20),
+    "shakhov_tetra3_nc9": (lambda d: cases.shakhov_cavity3d(d, "tetra", 3, 9, 0.5, 0.15, 20, gradient=False), 20),
+    # the residual check and the 10-check convergence counter: both stop with run_state 0 by convergence
+    "cdugks_q8_converge": (lambda d: _with_key(cases.bgk_cavity(d, 8, 100000), "residual-limit", "1e-05"), 100000),
+    "shakhov_q8_converge": (lambda d: cases.shakhov_cavity(d, "quad", 8, "hgh", 8, 0.1, 0.15, 100000), 100000),
+})
+OUTPUT = ("out_shakhov_q8", "out_cdugks_q8")
+RESTART = ("restart_shakhov_q8", "restart_cdugks_q8")
 
 
 def read_macros(path: str) -> dict:
@@ -105,21 +178,66 @@ def read_mesh(path: str) -> dict:
                 sym=np.array(sym, np.int32), dvs_max_magnitude=vmax)
 
 
+def _case_name(case_path: str) -> str:
+    for line in open(case_path):
+        t = line.split()
+        if len(t) >= 2 and t[0] == "case-name":
+            return t[1]
+    return "unnamed"
+
+
+def _set_key(case_path: str, key: str, value: str) -> None:
+    lines = open(case_path).read().splitlines()
+    out, done = [], False
+    for line in lines:
+        t = line.split()
+        if t and t[0] == key:
+            out.append(f"{key} {value}")
+            done = True
+        else:
+            out.append(line)
+            if not done and t and t[0] == "[settings]":
+                out.append(f"{key} {value}")
+                done = True
+    open(case_path, "w").write("\n".join(out) + "\n")
+
+
 def main() -> None:
     if not os.path.exists(REF):
         sys.exit("oracle/_ref/meso_ref missing: run oracle/build_ref.sh first")
     os.makedirs(CASE_DIR, exist_ok=True)
+    only = set(sys.argv[1:])
     for name, (build, steps) in GOLDEN.items():
+        if only and name not in only:
+            continue
         d = os.path.join(CASE_DIR, name)
         if os.path.isdir(d):
             shutil.rmtree(d)
         path = build(d)
-        args = [REF, os.path.basename(path), str(steps), "out.bin"]
+        inputs = set(os.listdir(d))  # files and folders the case reads (not the reference's output)
+        cname = _case_name(path)
+        args = [REF, os.path.relpath(path, d), str(steps), "out.bin"]
         if name in GEOMETRY:
             args += ["--mesh", "mesh.bin"]
+        if name in OUTPUT or name in RESTART:
+            args += ["--output", "1"]
         r = subprocess.run(args, cwd=d, capture_output=True, text=True)
         if r.returncode != 0:
             raise SystemExit(f"{name}: reference failed: {r.stderr}")
+        if name in OUTPUT:  # keep the reference's output() files
+            dst = os.path.join(HERE, "output", name)
+            if os.path.isdir(dst):
+                shutil.rmtree(dst)
+            shutil.copytree(os.path.join(d, cname), dst)
+        if name in RESTART:  # second run from the first run's latest/ files
+            _set_key(path, "read-np-data", "True")
+            r = subprocess.run(args[:4], cwd=d, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise SystemExit(f"{name}: reference restart failed: {r.stderr}")
+            for sub in os.listdir(os.path.join(d, cname)):  # keep only the restart inputs
+                if sub != "latest":
+                    p = os.path.join(d, cname, sub)
+                    shutil.rmtree(p) if os.path.isdir(p) else os.remove(p)
         m = read_macros(os.path.join(d, "out.bin"))
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), requested=steps, **m)
         if name in GEOMETRY:
@@ -128,8 +246,8 @@ def main() -> None:
         for junk in ("out.bin", "mesh.bin"):
             if os.path.exists(os.path.join(d, junk)):
                 os.remove(os.path.join(d, junk))
-        for sub in os.listdir(d):  # the reference's output folder (case-name/)
-            if os.path.isdir(os.path.join(d, sub)):
+        for sub in os.listdir(d):  # the reference's output folder (case-name/), except restart inputs
+            if sub not in inputs and os.path.isdir(os.path.join(d, sub)) and not (name in RESTART and sub == cname):
                 shutil.rmtree(os.path.join(d, sub))
         print(f"{name}: step {m['step']} run_state {m['run_state']}")
 

@@ -18,25 +18,33 @@ import pytest
 import cases
 import meso_gpu as mg
 from conftest import GOLDEN
-from helpers import max_field_err, relerr, run_gpu, run_oracle
+from helpers import (RESTART_GOLDENS, copy_golden_case, golden_case, golden_names, max_field_err, relerr,
+                     run_gpu, run_gpu_case_initial, run_oracle)
 
 TOL = 1e-12
 THRESHOLD_SENSITIVE = {"shakhov_q8_limiter"}
-GOLDEN_NAMES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("geometry_"))
+# the BGK solvers have no temperature or heat flux: their T and q fields are zero on both sides
+GOLDEN_NAMES = golden_names()
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", GOLDEN_NAMES)
-def test_fp64_matches_reference_outputs(gpu, name):
+def test_fp64_matches_reference_outputs(gpu, name, tmp_path):
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
-    path = os.path.join(GOLDEN, "cases", name, "case.txt")
+    path = golden_case(name)
     steps = int(g["requested"])
+    if name in RESTART_GOLDENS:  # initial() from the first run's latest/ files (read-np-data True)
+        r = run_gpu_case_initial(copy_golden_case(name, str(tmp_path / name)), steps, mg.FP64)
+        assert r["step"] == int(g["step"])
+        for k in ("rho", "u", "T", "q"):
+            assert relerr(r[k], g[k]) <= TOL, (k, relerr(r[k], g[k]))
+        return
     try:
         r = run_gpu(path, steps, mg.FP64)
     except mg.MesoError as e:
         # the reference stopped on a NaN / T<0 cell: the GPU must stop at the same step
         assert e.code == mg.ERR_NAN and int(g["run_state"]) == 0
-        s = mg.Solver(os.path.join(GOLDEN, "cases", name, "case.txt"), mg.FP64)
+        s = mg.Solver(path, mg.FP64)
         s.initial()
         with pytest.raises(mg.MesoError):
             s.step(steps)
@@ -44,7 +52,7 @@ def test_fp64_matches_reference_outputs(gpu, name):
         assert st.step == int(g["step"]) and st.run_state == 0 and st.bad_cells > 0
         s.close()
         return
-    assert r["step"] == int(g["step"])
+    assert r["step"] == int(g["step"]) and r["run_state"] == int(g["run_state"])
     tol = dict.fromkeys(("rho", "u", "T", "q"), TOL)
     if name in THRESHOLD_SENSITIVE:
         # The Venkatakrishnan limiter returns 1 when |dw| <= eps (limiter.cpp:11), a jump that turns
@@ -53,8 +61,18 @@ def test_fp64_matches_reference_outputs(gpu, name):
         # GPU must stay inside 4x that envelope.
         o2 = run_oracle(path, steps, nthreads=2)
         tol = {k: max(TOL, 4.0 * relerr(o2[k], g[k])) for k in tol}
-    for k in ("rho", "u", "T", "q"):
+    for k in ("rho", "u", "T"):
         assert relerr(r[k], g[k]) <= tol[k], (k, relerr(r[k], g[k]), tol[k])
+    assert q_err(r["q"], g, mg.Case(path).params.R) <= tol["q"], (q_err(r["q"], g, mg.Case(path).params.R), tol["q"])
+
+
+def q_err(q, g, R: float) -> float:
+    """Heat-flux error: max |q - q_ref| over max |q_ref|, where q_ref is at least 1 % of the size
+    rho (R T)^(3/2) of the terms of its velocity sum.  In near-continuum cases (ref_re1000: Kn 1.8e-4)
+    the heat flux itself is a thousand times smaller than its terms, and its last bits are the
+    rounding of their sum."""
+    scale = max(float(np.max(np.abs(g["q"]))), 0.01 * float(np.max(g["rho"])) * (R * float(np.max(g["T"]))) ** 1.5)
+    return float(np.max(np.abs(np.asarray(q) - g["q"]))) / scale if scale > 0 else 0.0
 
 
 CASES = [

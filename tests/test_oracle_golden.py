@@ -13,19 +13,22 @@ import pytest
 
 import meso_gpu as mg
 from conftest import GOLDEN
-from helpers import relerr, run_oracle
+from helpers import HEAVY_GOLDENS, RESTART_GOLDENS, golden_case, golden_names, relerr, run_oracle, run_oracle_restart
 
-NAMES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("geometry_"))
+NAMES = golden_names()
 
 
 def _case(name):
-    return os.path.join(GOLDEN, "cases", name, "case.txt")
+    return golden_case(name)
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", [n for n in NAMES if n not in HEAVY_GOLDENS])
 def test_oracle_bit_exact(name):
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
-    o = run_oracle(_case(name), int(g["requested"]))
+    if name in RESTART_GOLDENS:
+        o = run_oracle_restart(_case(name), int(g["requested"]))
+    else:
+        o = run_oracle(_case(name), int(g["requested"]))
     assert o["step"] == int(g["step"])
     assert o["run_state"] == int(g["run_state"])
     for k in ("rho", "u", "T", "q"):
