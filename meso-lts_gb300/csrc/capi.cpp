@@ -854,6 +854,16 @@ int meso_case_loop_settings(const meso_case *c, int32_t *max_step, int32_t *writ
     return MESO_OK;
 }
 
+int meso_case_output_grid(const meso_case *c, const char *path) {
+    if (!c || !path) return fail(MESO_ERR_INVALID, "null argument");
+    try {
+        write_grid(*c, path);
+    } catch (const std::exception &e) {
+        return fail(MESO_ERR_IO, e.what());
+    }
+    return MESO_OK;
+}
+
 int meso_ctx_create(const meso_mesh_desc *mesh, const meso_dvs_desc *dvs, const meso_mark_desc *marks, int32_t nmarks,
                     const meso_params *params, const uint8_t *mask, meso_ctx **out) {
     if (!out || !params) return fail(MESO_ERR_INVALID, "null argument");
@@ -998,6 +1008,10 @@ int meso_step(meso_ctx *c, int32_t nsteps, int32_t *steps_done) {
         (rc = meso_host::ctx_read_resid(c)))
         return rc;
     if (steps_done) *steps_done = done;
+    if (c->h_status->timeout) {
+        c->run_state = 0;
+        return fail(MESO_ERR_TIMEOUT, "a bounded device wait gave up: the last step's results are invalid");
+    }
     if (stopped || c->h_status->stop_step != INT_MAX) {
         c->run_state = 0;
         return fail(MESO_ERR_NAN, "cell " + std::to_string(c->rn.cell_new2old[std::min(c->h_status->first_bad, c->C - 1)]) +
