@@ -162,13 +162,18 @@ int device_setup(DeviceSlot &out) {
     return MESO_OK;
 }
 
-bool on_device(const void *p) {
+// Where a caller's pointer lives.  0: device (or managed) memory of device `dev`; 1: anything else
+// (pageable or page-locked host memory, another GPU's memory, an unknown address).  An error that
+// the attribute query itself raises is this call's own (the entry point refuses to run while an
+// earlier error is pending), so it is cleared here.
+int where(const void *p, int dev) {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return 1;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return 0;
+    return a.type == cudaMemoryTypeDevice && a.device == dev ? 0 : 1;
 }
 
 }  // namespace
@@ -182,10 +187,25 @@ extern "C" int meso_shakhov_moments_noalloc(const double *g, const double *h, in
                                                       " exceeds MESO_NOALLOC_MAX_CELLS = " + std::to_string(kMaxCells));
     if (dim != 2 && dim != 3) return meso_host::fail(MESO_ERR_INVALID, "dim must be 2 or 3");
     if (!(R > 0.0) || !(K >= 0.0)) return meso_host::fail(MESO_ERR_INVALID, "R must be > 0 and K >= 0");
+    // An error left pending by earlier CUDA work of the caller stays theirs to read: it is neither
+    // cleared here nor reported as this call's launch failure.
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending == cudaErrorNoDevice || pending == cudaErrorInsufficientDriver)  // no GPU to hold the arrays
+        return meso_host::fail(MESO_ERR_INVALID, std::string("no usable CUDA device (") + cudaGetErrorString(pending) +
+                                                     "): the arrays cannot be device memory of the current GPU");
+    if (pending != cudaSuccess)
+        return meso_host::fail(MESO_ERR_CUDA, std::string("a CUDA error is pending from before this call: ") +
+                                                  cudaGetErrorString(pending));
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        dev = -1;
+    }
     const void *ptrs[] = {g, h, xi, w, u0, rho, u, T, q};
     for (const void *p : ptrs)
-        if (!p || !on_device(p))
-            return meso_host::fail(MESO_ERR_INVALID, "every array must be device (or managed) memory of this GPU");
+        if (!p || where(p, dev) != 0)
+            return meso_host::fail(MESO_ERR_INVALID,
+                                   "every array must be device (or managed) memory of the current GPU");
     DeviceSlot slot;
     int rc = device_setup(slot);
     if (rc) return rc;
@@ -199,6 +219,11 @@ extern "C" int meso_shakhov_moments_noalloc(const double *g, const double *h, in
     ngroup = ngroup < fit ? ngroup : fit;
     ngroup = ngroup < 65535 ? ngroup : 65535;
     ngroup = ngroup > 1 ? ngroup : 1;
+    // no empty group: with per = ceil(nv / ngroup) velocities each, ceil(nv / per) groups cover nv
+    {
+        const int per = (nv + ngroup - 1) / ngroup;
+        ngroup = (nv + per - 1) / per;
+    }
     // the counters must start at zero; the partials need no clearing (each is written before it is read)
     cudaError_t e = cudaMemsetAsync(slot.scratch, 0, sizeof(unsigned) * (size_t)ncb, st);
     if (e != cudaSuccess) return meso_host::fail(MESO_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));

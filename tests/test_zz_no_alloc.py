@@ -125,6 +125,129 @@ def test_noalloc_moments_match_init_macros(gpu, tmp_path):
         buf.close()
 
 
+def _numpy_moments(g, h, xi, w, u0, R, K, dim):
+    """The same sums in numpy (FP64): rho, u, T, q of a state, heat flux about u0."""
+    rho = g @ w
+    mom = (g * w[None, :]) @ xi[:, :dim]
+    u = np.zeros((g.shape[0], 3))
+    u[:, :dim] = mom / rho[:, None]
+    kk = np.sum(xi[:, :dim] ** 2, axis=1)
+    rhoE = 0.5 * ((g * kk[None, :] + h) @ w)
+    Cv = (K + 3.0) * R * 0.5
+    T = (rhoE / rho - 0.5 * np.sum(u * u, axis=1)) / Cv
+    c = xi[None, :, :dim] - u0[:, None, :dim]
+    s = np.sum(c * c, axis=-1) * g + h
+    q = np.zeros((g.shape[0], 3))
+    q[:, :dim] = 0.5 * np.einsum("cpd,cp,p->cd", c, s, w)
+    qs = 0.5 * np.einsum("cpd,cp,p->d", np.abs(c), np.abs(s), w).max()
+    return rho, u, T, q, qs
+
+
+def _tensor_set(n: int, dim: int, lim: float):
+    """A Newton-Cotes-like tensor velocity set on [-lim, lim]^dim (trapezoid weights)."""
+    x = np.linspace(-lim, lim, n)
+    wx = np.full(n, x[1] - x[0])
+    wx[0] = wx[-1] = 0.5 * (x[1] - x[0])
+    grids = np.meshgrid(*([x] * dim), indexing="ij")
+    wg = np.meshgrid(*([wx] * dim), indexing="ij")
+    xi = np.zeros((n ** dim, 3))
+    for d in range(dim):
+        xi[:, d] = grids[d].reshape(-1)
+    w = np.prod(np.stack([a.reshape(-1) for a in wg]), axis=0)
+    return xi, w
+
+
+def _maxwell(rho, u, T, xi, R, K, dim):
+    c = xi[None, :, :dim] - u[:, None, :dim]
+    cc = np.sum(c * c, axis=-1)
+    RT = R * T
+    g = rho[:, None] / (2.0 * np.pi * RT[:, None]) ** (dim / 2.0) * np.exp(-cc / (2.0 * RT[:, None]))
+    h = (K + 3.0 - dim) * RT[:, None] * g
+    return g, h
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim,ncell,nside,lim", [(3, 300, 13, 4.0), (2, 131072, 3, 1.7320508075688772)])
+def test_noalloc_moments_match_numpy(gpu, dim, ncell, nside, lim):
+    """3-D states, and the largest accepted cell count (one velocity group: the partials fill the
+    scratch array), against the same sums evaluated in numpy, two calls in a row."""
+    lib = mg.lib()
+    R, K = 0.5, 1.0
+    xi, w = _tensor_set(nside, dim, lim)
+    nv = xi.shape[0]
+    buf = DeviceBuffers()
+    try:
+        for call in range(2):
+            rng = np.random.default_rng(10 * dim + call)
+            rho = 1.0 + 0.2 * (rng.random(ncell) - 0.5)
+            T = 1.0 + 0.3 * (rng.random(ncell) - 0.5)
+            u = np.zeros((ncell, 3))
+            u[:, :dim] = 0.2 * (rng.random((ncell, dim)) - 0.5)
+            u0 = u + 0.05 * (rng.random((ncell, 3)) - 0.5)
+            u0[:, dim:] = 0.0
+            g, h = _maxwell(rho, u, T, xi, R, K, dim)
+            g *= 1.0 + 0.01 * (rng.random(g.shape) - 0.5)  # off equilibrium: non-zero heat flux
+            ref = _numpy_moments(g, h, xi, w, u0, R, K, dim)
+            outs = [buf.empty(ncell), buf.empty(3 * ncell), buf.empty(ncell), buf.empty(3 * ncell)]
+            rc = lib.meso_shakhov_moments_noalloc(buf.put(g), buf.put(h), ncell, nv, dim, buf.put(xi), buf.put(w),
+                                                  buf.put(u0), R, K, *outs, None)
+            assert rc == mg.OK, lib.meso_last_error().decode()
+            buf.sync()
+            got = (buf.get(outs[0], ncell), buf.get(outs[1], 3 * ncell).reshape(ncell, 3), buf.get(outs[2], ncell),
+                   buf.get(outs[3], 3 * ncell).reshape(ncell, 3))
+            errs = {"rho": relerr(got[0], ref[0]), "u": relerr(got[1], ref[1]), "T": relerr(got[2], ref[2]),
+                    "q/terms": float(np.max(np.abs(got[3] - ref[3])) / ref[4])}
+            print(dim, ncell, nv, call, errs)
+            for key, e in errs.items():
+                assert e <= TOL, (dim, ncell, call, key, e)
+            buf.close()
+    finally:
+        buf.close()
+
+
+@pytest.mark.gpu
+def test_noalloc_moments_match_oracle(gpu, tmp_path):
+    """The oracle's initial() moments of a mode-0 state (cdugks_shakhov.cpp:102-169) against the
+    entry point on the same state, built in numpy."""
+    import meso_oracle as mo
+
+    lib = mg.lib()
+    buf = DeviceBuffers()
+    try:
+        case = mg.Case(_case(tmp_path, "nc21_20"))
+        n, nv = case.ncell, case.nv
+        rho, u, T, g, h, xi, w, R, K, q_scale = _equilibrium_state(case, seed=7)
+        o = mo.Oracle(case, 1)
+        o.init(rho, u, T, None, 0)
+        ref = o.macros()
+        o.close()
+        outs = [buf.empty(n), buf.empty(3 * n), buf.empty(n), buf.empty(3 * n)]
+        rc = lib.meso_shakhov_moments_noalloc(buf.put(g), buf.put(h), n, nv, 2, buf.put(xi), buf.put(w), buf.put(u),
+                                              R, K, *outs, None)
+        assert rc == mg.OK, lib.meso_last_error().decode()
+        buf.sync()
+        got = (buf.get(outs[0], n), buf.get(outs[1], 3 * n).reshape(n, 3), buf.get(outs[2], n),
+               buf.get(outs[3], 3 * n).reshape(n, 3))
+        errs = {"rho": relerr(got[0], ref[0]), "u": relerr(got[1], ref[1]), "T": relerr(got[2], ref[2]),
+                "q/terms": float(np.max(np.abs(got[3] - ref[3])) / np.max(q_scale))}
+        print(errs)
+        for key, e in errs.items():
+            assert e <= TOL, (key, e)
+    finally:
+        buf.close()
+
+
+def test_noalloc_rejects_host_memory():
+    """A pageable host array is not device memory of the current GPU: MESO_ERR_INVALID, on a
+    machine with or without a GPU."""
+    lib = mg.lib()
+    a = np.zeros(64)
+    pa = a.ctypes.data
+    rc = lib.meso_shakhov_moments_noalloc(pa, pa, 4, 9, 2, pa, pa, pa, 0.5, 0.0, pa, pa, pa, pa, None)
+    assert rc == mg.ERR_INVALID, rc
+    assert "device" in lib.meso_last_error().decode()
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     """Host-side checks, before any device work: no GPU needed."""
     lib = mg.lib()
