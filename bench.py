@@ -493,7 +493,7 @@ def run_profile(args) -> int:
                 case.close()
             return 0
         build = {"config1": lambda p: cases.config1(p, 10),
-                 "config2": lambda p: cases.config2(p, 10, args.precision),
+                 "config2": lambda p: cases.config2(p, 10, args.precision, nv1d=args.nv1d or 101),
                  "config3": lambda p: cases.config3(p, 10, args.precision)}[args.profile]
         case = mg.Case(build(os.path.join(d, args.profile)))
         rho, u, T, mask = case.initial_fields()
@@ -525,6 +525,8 @@ def main() -> int:
                     help="run a few steps of one workload for a profiler capture and exit")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="with --profile")
     ap.add_argument("--phases", action="store_true", help="with --profile: per-phase device times")
+    ap.add_argument("--nv1d", type=int, default=0,
+                    help="with --profile config2: Newton-Cotes points per axis (a smaller case for ncu captures)")
     args = ap.parse_args()
     if args.profile:
         _cudart().cudaSetDevice(dist_env()[2])
