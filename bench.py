@@ -41,6 +41,7 @@ from __future__ import annotations
 import argparse
 import ctypes
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -123,15 +124,16 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu: int):
+    def __init__(self, gpu: int, interval_ms: int = 50):
         self.gpu = gpu
+        self.interval_ms = interval_ms
         self.proc = None
         self.lines: list[str] = []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.interval_ms)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -241,9 +243,9 @@ def run_reference(args, rank: int, dist: Dist) -> None:
     with tempfile.TemporaryDirectory() as tmp:
         path = build_workload(tmp, "fp64")
         threads = os.cpu_count() or 1
-        # bounded: a config-2 step takes about 0.7 s on 16 Grace cores, so at most 10 timed steps
-        # after 3 to 5 warm-up steps keep the run within a few minutes on any host
-        steps = max(1, min(args.steps, 10))
+        # the same step count as the GPU arm, bounded: a step takes about 0.65 s on 16 Grace cores, so
+        # at most 200 timed steps after 3 to 5 warm-up steps keep the run within a few minutes
+        steps = max(1, min(args.steps, 200))
         warm = max(3, min(args.warmup, 5))
         import meso_gpu as mg
         import meso_oracle as mo
@@ -263,8 +265,8 @@ def run_reference(args, rank: int, dist: Dist) -> None:
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "cells": case.ncell, "velocities": case.nv},
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                 "sample": f"{done} of the requested {args.steps} steps (bounded), "
-                                           f"{warm} warm-up step(s), {threads} threads"},
+                                 "sample": f"{done} timed steps (requested {args.steps}, at most 200) of the full "
+                                           f"workload after {warm} warm-up step(s), {threads} threads"},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
 
@@ -303,20 +305,27 @@ def run_other_configs(tmp: str) -> dict:
     c3 = mg.Case(p3)
     rho, u, T, mask = c3.initial_fields()
     res = {}
-    for prec in (mg.FP32, mg.FP64):
+    for prec in (mg.FP32, mg.FP64):  # the workload's 5000 steps; 200 of them timed
         s = mg.Solver(case=c3, precision=prec, mask=mask)
         s.init_macros(rho, u, T, None, 0)
         s.step(3)
         s.step(200)
-        res[prec] = (s.last_step_ms() / 200, s.macros(c3.ncell))
+        ms = s.last_step_ms() / 200
+        s.step(4900 - 203)
+        before = s.macros(c3.ncell)
+        s.step(100)
+        res[prec] = (ms, s.macros(c3.ncell), before, s.status().step)
         s.close()
     cx3 = c3.ncell * c3.nv
-    out["config3_shakhov_fp32"] = {"cells": c3.ncell, "velocities": c3.nv, "steps": 203,
+    comps = lambda a: {"rho": a[0], "T": a[2], "u": a[1][:, 0], "v": a[1][:, 1], "qx": a[3][:, 0], "qy": a[3][:, 1]}
+    e32 = {k: relerr(comps(res[mg.FP32][1])[k], v) for k, v in comps(res[mg.FP64][1]).items()}
+    drift = {k: relerr(comps(res[mg.FP64][2])[k], v) for k, v in comps(res[mg.FP64][1]).items()}
+    out["config3_shakhov_fp32"] = {"cells": c3.ncell, "velocities": c3.nv, "steps": res[mg.FP32][3],
                                    "value": cx3 / (res[mg.FP32][0] * 1e-3), "unit": UNIT,
                                    "ms_per_step": res[mg.FP32][0], "fp64_ms_per_step": res[mg.FP64][0],
-                                   "fp32_error_vs_fp64": {k: relerr(x, y) for k, x, y in
-                                                          zip(("rho", "u", "T", "q"), res[mg.FP32][1], res[mg.FP64][1])},
-                                   "note": "state 23 MB fits in L2"}
+                                   "fp32_error_vs_fp64": e32, "fp64_change_steps_4900_5000": drift,
+                                   "note": "state 23 MB fits in L2; CFL 0.5 (at 0.8 the reference blows up at step "
+                                           "140, tests/golden/config3_cfl08_blowup.npz)"}
     return out
 
 
@@ -510,6 +519,108 @@ def run_profile(args) -> int:
     return 0
 
 
+def run_served_config5(tmp: str, count: int = 40, rate: float = 20.0, max_step: int = 3000, poll_steps: int = 100,
+                       members: int = 64, fp64_sample: int = 3, fp64_budget_s: float = 30.0) -> dict:
+    """The served stream drawn from the batch workload's distribution (sides {32,48,64,96,128} quads,
+    DVS {D2Q9, hGH 28^2, NC 101^2}, log10 Kn ~ U(-2,0), lid ~ U(.05,.15)), Poisson arrivals at 20/s
+    (seed 2), bounded to `count` requests and `max_step` steps each.  Time-to-converged over the
+    solves that converged; capped and failed (NaN) solves counted apart.  Serial plain FP64 is measured
+    (not estimated) on a seeded sample of the requests, each run alone to the same stopping rule,
+    within a wall-time budget."""
+    import cases
+    import meso_gpu as mg
+
+    reqs = cases.config5_requests(count=count, rate=rate, sides=(32, 48, 64, 96, 128), dvs_kinds=("d2q9", "hgh", "nc"))
+    paths, params = [], []
+    for r in reqs:
+        p = cases.config5_case(os.path.join(tmp, f"c5_{r['index']}"), r, max_step, nc_points=101)
+        prm = mg.Case(p).params
+        prm.residual_interval = 100
+        prm.residual_limit = 1e-6
+        prm.residual_fields = mg.RES_U | mg.RES_L2
+        paths.append(p)
+        params.append(prm)
+    rt = _cudart()
+    free_b, total_b = ctypes.c_size_t(), ctypes.c_size_t()
+    rt.cudaMemGetInfo(ctypes.byref(free_b), ctypes.byref(total_b))
+    srv = mg.Server(hbm_budget_bytes=int(free_b.value * 0.8), max_members=members)
+    done = {}
+    i = 0
+    t0 = time.perf_counter()
+    while len(done) < count:
+        now = time.perf_counter() - t0
+        while i < count and reqs[i]["arrival"] <= now:
+            srv.submit(paths[i], params[i])
+            i += 1
+        pend, run, _ = srv.counts()
+        if pend + run == 0:
+            time.sleep(max(0.0, min(0.01, reqs[i]["arrival"] - now)) if i < count else 0.0)
+            continue
+        for t in srv.poll(poll_steps):
+            _, st, sec = srv.result(t)
+            done[t] = dict(step=st.step, converged=st.converged, run_state=st.run_state, bad=st.bad_cells,
+                           latency=sec[0])
+            srv.release(t)
+    wall = time.perf_counter() - t0
+    gpu_ms, poll_ms, batch_steps = srv.stats()
+    srv.close()
+    res = [done[k] for k in sorted(done)]  # tags follow submission order
+    conv = [r for r in res if r["converged"]]
+    failed = [r for r in res if not r["converged"] and r["bad"] > 0]
+    capped = [r for r in res if not r["converged"] and r["bad"] == 0]
+    lat = sorted(r["latency"] for r in conv)
+    q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))] if lat else None
+    # serial plain FP64 on a seeded sample, each alone, the same stopping rule
+    rng = np.random.default_rng(5)
+    sample = sorted(int(x) for x in rng.choice(count, size=min(fp64_sample, count), replace=False))
+    fp64 = []
+    t_budget = time.perf_counter()
+    for k in sample:
+        if time.perf_counter() - t_budget > fp64_budget_s:
+            fp64.append({"request": k, "skipped": "over the wall-time budget"})
+            continue
+        case = mg.Case(paths[k])
+        rho, u, T, mask = case.initial_fields()
+        prm = params[k]
+        prm.precision = mg.FP64
+        s = mg.Solver(case=case, precision=mg.FP64, mask=mask, params=prm)
+        s.init_macros(rho, u, T, None, 0)
+        t1 = time.perf_counter()
+        n = 0
+        try:
+            while n < max_step and time.perf_counter() - t1 < fp64_budget_s:
+                got = s.step(min(poll_steps, max_step - n))
+                n += got
+                if got == 0 or s.status().run_state == 0:
+                    break
+        except mg.MesoError:
+            pass
+        secs = time.perf_counter() - t1
+        st = s.status()
+        s.close()
+        case.close()
+        fp64.append({"request": k, "cells": reqs[k]["side"] ** 2, "dvs": reqs[k]["dvs"], "steps": st.step,
+                     "converged": st.converged, "seconds": secs,
+                     "served_seconds": res[k]["latency"], "served_steps": res[k]["step"]})
+    timed = [x for x in fp64 if "seconds" in x]
+    return {"workload": f"{count} cavity solves drawn like the batch workload: sides {{32,48,64,96,128}} quads, "
+                        "log10 Kn ~ U(-2,0), DVS {D2Q9, hGH 28x28, NC 101x101}, lid ~ U(0.05,0.15), Poisson arrivals "
+                        f"{rate}/s (seed 2), FP32 storage, run to L2-relative residual 1e-6 on U per 100 steps, "
+                        f"at most {max_step} steps",
+            "max_members": members, "solves_per_s": count / wall, "wall_seconds": wall, "batch_steps": batch_steps,
+            "gpu_seconds": gpu_ms * 1e-3, "converged": len(conv), "capped": len(capped), "failed_nan": len(failed),
+            "p50_s_converged": q(0.50), "p99_s_converged": q(0.99),
+            "mean_steps_converged": float(np.mean([r["step"] for r in conv])) if conv else None,
+            "by_dvs": {d: {"converged": sum(1 for r, x in zip(reqs, res) if r["dvs"] == d and x["converged"]),
+                           "capped": sum(1 for r, x in zip(reqs, res) if r["dvs"] == d and not x["converged"]
+                                         and x["bad"] == 0),
+                           "failed_nan": sum(1 for r, x in zip(reqs, res) if r["dvs"] == d and x["bad"] > 0)}
+                       for d in ("d2q9", "hgh", "nc")},
+            "serial_fp64_sample": fp64,
+            "serial_fp64_solves_per_s_sample": (len(timed) / sum(x["seconds"] for x in timed)) if timed else None,
+            "served_solves_per_s_same_sample": (len(timed) / sum(x["served_seconds"] for x in timed)) if timed else None}
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -521,6 +632,8 @@ def main() -> int:
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--served-count", type=int, default=200)
     ap.add_argument("--served-members", type=int, default=64, help="solves stepped together at most")
+    ap.add_argument("--served5-count", type=int, default=40,
+                    help="requests of the served stream drawn from the batch workload's distribution")
     ap.add_argument("--profile", choices=["config1", "config2", "config3", "served64"],
                     help="run a few steps of one workload for a profiler capture and exit")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="with --profile")
@@ -551,19 +664,29 @@ def main() -> int:
         cx = C * NV
         K, W = args.steps, args.warmup
 
-        # ---- device-timed FP32 step, state resident
+        # ---- device-timed FP32 step, state resident.  Blocks of exactly K steps, each bracketed by a
+        # barrier and synchronisations and timed with CUDA events on the library's stream, repeated
+        # until about a second has passed so that the clock record covers the timed region; the
+        # median block is reported (all ranks run the same number of blocks)
         s = mg.Solver(case=case, precision=mg.FP32, mask=mask)
         s.init_macros(rho, u, T, None, 0)
         s.step(W)
-        dist.barrier()
-        rt.cudaDeviceSynchronize()
+        block_ms, ok = [], True
         with ClockSampler(local) as clk:
-            done = s.step(K)
-            rt.cudaDeviceSynchronize()
-        ms = s.last_step_ms()
+            reps = 1
+            while len(block_ms) < reps:
+                dist.barrier()
+                rt.cudaDeviceSynchronize()
+                done = s.step(K)
+                rt.cudaDeviceSynchronize()
+                block_ms.append(s.last_step_ms())
+                ok = ok and done == K
+                if len(block_ms) == 1:
+                    reps = int(dist.max(float(min(200, max(1, math.ceil(1000.0 / max(block_ms[0], 1e-3)))))))
+        ms = statistics.median(block_ms)
         launches = s.last_step_launches()
         st = s.status()
-        ok = done == K and st.run_state == 1
+        ok = ok and st.run_state == 1
         ms_max = dist.max(ms)
         total_cx = dist.sum(float(cx * K))
         value = total_cx / (ms_max * 1e-3)
@@ -572,16 +695,20 @@ def main() -> int:
         fp32_macros = None
         s.close()
 
-        # ---- plain FP64 step on the same workload (fewer steps: it is ~8x slower)
-        K64 = max(3, K // 10)
+        # ---- plain FP64 step on the same workload, run for the workload's 500 steps (K64 of them
+        # timed), and the FP32 form's error against it there; the FP64 fields' own change over the
+        # last 100 steps shows how far from steady state step 500 is
+        K64 = max(3, min(K, 50))
+        nerr = 500
         s64 = mg.Solver(case=case, precision=mg.FP64, mask=mask)
         s64.init_macros(rho, u, T, None, 0)
         s64.step(1)
         s64.step(K64)
         ms64 = s64.last_step_ms()
         fp64_value = cx * K64 / (ms64 * 1e-3)
-        # error of the FP32 form against FP64 after the same number of steps
-        nerr = 1 + K64
+        s64.step(nerr - 100 - 1 - K64)
+        b400 = s64.macros(C)
+        s64.step(100)
         b = s64.macros(C)
         s64.close()
         s32 = mg.Solver(case=case, precision=mg.FP32, mask=mask)
@@ -590,6 +717,7 @@ def main() -> int:
         a = s32.macros(C)
         s32.close()
         err = {k: relerr(x, y) for k, x, y in zip(("rho", "u", "T", "q"), a, b)}
+        err["fp64_change_steps_400_500"] = {k: relerr(x, y) for k, x, y in zip(("rho", "u", "T", "q"), b400, b)}
 
         # ---- e2e through the C ABI with pinned host buffers
         hr, hu, hT = pinned(C), pinned(3 * C), pinned(C)
@@ -626,10 +754,12 @@ def main() -> int:
         traffic, traffic_note = ncu_traffic(dom)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
-            "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": ms_max / K, "timed_blocks": len(block_ms), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None,
             "dtype": "f32 (FP64 moments and equilibria)", "data": "synthetic",
             "config": {"workload": WORKLOAD, "cells": C, "velocities": NV, "state_bytes": 16 * cx,
                        "l2": "state (1.3 GB, two buffers) larger than L2; no flush needed",
+                       "timing": f"median of {len(block_ms)} blocks of {K} steps (CUDA events per block)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "run_ok": ok,
             "fp64_value": fp64_value, "fp64_ms_per_step": ms64 / K64, "fp32_over_fp64": value / world / fp64_value,
@@ -652,6 +782,7 @@ def main() -> int:
             line["batched"] = run_batched(tmp)
         if not args.no_served:
             line["served"] = run_served(tmp, count=args.served_count, members=args.served_members)
+            line["served_config5"] = run_served_config5(tmp, count=args.served5_count, members=args.served_members)
         if rank == 0:
             print(json.dumps(line), flush=True)
     dist.close()

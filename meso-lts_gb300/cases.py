@@ -617,8 +617,10 @@ def config5_requests(seed: int = 2, count: int = 200, rate: float = 20.0,
     return out
 
 
-def config5_case(d: str, req: dict, max_step: int = 4000) -> str:
-    nv1d = {"d2q9": 3, "hgh": 28, "nc": 21}[req["dvs"]]
+def config5_case(d: str, req: dict, max_step: int = 4000, nc_points: int = 21) -> str:
+    """One served request's case: NC nc_points^2 (21 in the scaled stream, 101 in the stream drawn from
+    the batch workload's distribution), hGH 28^2 or D2Q9; CFL 0.5."""
+    nv1d = {"d2q9": 3, "hgh": 28, "nc": nc_points}[req["dvs"]]
     return shakhov_cavity(d, "quad", req["side"], req["dvs"], nv1d, req["kn"], req["lid"], max_step,
                           name=f"req{req['index']}", precision="fp32", cfl=0.5)
 
