@@ -58,7 +58,9 @@ def _errs(a, b):
 def test_config3_fp32_5000_steps_against_fp64(gpu, config3_path):
     """The FP32 error after the workload's 5000 steps, printed beside the FP64 fields' own change over
     the last 100 steps (how far step 5000 is from the steady state of the 1e-6 bar).  Measured:
-    rho 2.7e-8, T 2.8e-8, u 1.3e-6, v 7.7e-7, qx 2.0e-5, qy 1.3e-5; bounded with a margin of 1.5."""
+    rho 2.7e-8, T 2.8e-8, u 1.3e-6, v 7.7e-7, qx 2.0e-5, qy 1.3e-5, while the FP64 fields still move
+    by rho 4.5e-5, T 1.1e-5, u 4.1e-4, v 1.6e-4 over steps 4900-5000: a transient error, bounded
+    here with a margin of 1.5."""
     a = _fields(config3_path, mg.FP32, [5000])[0]
     b4900, b = _fields(config3_path, mg.FP64, [4900, 5000])
     errs = _errs(a, b)
