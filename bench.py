@@ -20,7 +20,10 @@ Metric: cell-velocity updates per second (cells x velocities x steps / time).
                and written in FP32; each launch covers every cell-velocity) /
                its event-timed duration, against the measured HBM copy bandwidth
   cpu_baseline the oracle (CPU restatement of the reference step) on all host
-               cores, on a bounded sample of the same workload
+               cores, on a bounded sample of the same workload, fed the
+               workload's mesh and velocity tables as the reference itself
+               builds them (tests/golden/workload_config2.npz), not through
+               the product library
 
 --impl reference times that CPU implementation alone (rank 0) on the same
 workload and prints the same JSON line with "impl": "reference".
@@ -212,14 +215,22 @@ def pinned(n: int):
     return np.frombuffer(buf, dtype=np.float64)
 
 
-def cpu_baseline(path: str, seconds: float, threads: int) -> dict:
-    import meso_gpu as mg
+WORKLOAD_TABLES = os.path.join(ROOT, "tests", "golden", "workload_config2.npz")
+
+
+def _oracle_workload(threads: int):
+    """The oracle on the workload's mesh and velocity tables as the reference builds them
+    (tests/golden/workload_config2.npz): the CPU legs load no part of the product library."""
     import meso_oracle as mo
 
-    case = mg.Case(path)
-    rho, u, T, mask = case.initial_fields()
-    o = mo.Oracle(case, threads, mask)
-    o.init(rho, u, T, None, 0)
+    w = mo.Workload(WORKLOAD_TABLES)
+    o = mo.Oracle(w, threads)
+    o.init(w.rho, w.u, w.T, None, 0)
+    return w, o
+
+
+def cpu_baseline(seconds: float, threads: int) -> dict:
+    w, o = _oracle_workload(threads)
     # one step to size the sample, then about `seconds` of steps (at most 30)
     t0 = time.perf_counter()
     done, _ = o.step(1)
@@ -230,45 +241,41 @@ def cpu_baseline(path: str, seconds: float, threads: int) -> dict:
     done += d2
     secs = first + (time.perf_counter() - t1)
     o.close()
-    cx = case.ncell * case.nv
+    cx = w.ncell * w.nv
     return {"value": cx * done / secs, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{done} full step(s) of the workload ({case.ncell} cells x {case.nv} velocities) on "
-                      f"{threads} threads, velocity set split as the reference's MPI ranks split it",
+            "sample": f"{done} full step(s) of the workload ({w.ncell} cells x {w.nv} velocities, the reference's own "
+                      f"mesh and velocity tables) on {threads} threads, velocity set split as the reference's MPI "
+                      "ranks split it",
             "seconds": secs}
 
 
 def run_reference(args, rank: int, dist: Dist) -> None:
     if rank != 0:
         return
-    with tempfile.TemporaryDirectory() as tmp:
-        path = build_workload(tmp, "fp64")
-        threads = os.cpu_count() or 1
-        # the same step count as the GPU arm, bounded: a step takes about 0.65 s on 16 Grace cores, so
-        # at most 200 timed steps after 3 to 5 warm-up steps keep the run within a few minutes
-        steps = max(1, min(args.steps, 200))
-        warm = max(3, min(args.warmup, 5))
-        import meso_gpu as mg
-        import meso_oracle as mo
-
-        case = mg.Case(path)
-        rho, u, T, mask = case.initial_fields()
-        o = mo.Oracle(case, threads, mask)
-        o.init(rho, u, T, None, 0)
-        o.step(warm)
-        t0 = time.perf_counter()
-        done, _ = o.step(steps)
-        secs = time.perf_counter() - t0
-        cx = case.ncell * case.nv
-        v = cx * done / secs
-        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": done, "warmup": warm, "ms_per_step": secs * 1e3 / done, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "cells": case.ncell, "velocities": case.nv},
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                 "sample": f"{done} timed steps (requested {args.steps}, at most 200) of the full "
-                                           f"workload after {warm} warm-up step(s), {threads} threads"},
-                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
+    threads = os.cpu_count() or 1
+    # the same step count as the GPU arm, bounded: a step takes about 0.65 s on 16 Grace cores, so
+    # at most 200 timed steps after 3 to 5 warm-up steps keep the run within a few minutes
+    steps = max(1, min(args.steps, 200))
+    warm = max(3, min(args.warmup, 5))
+    w, o = _oracle_workload(threads)
+    o.step(warm)
+    t0 = time.perf_counter()
+    done, _ = o.step(steps)
+    secs = time.perf_counter() - t0
+    o.close()
+    cx = w.ncell * w.nv
+    v = cx * done / secs
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": done, "warmup": warm, "ms_per_step": secs * 1e3 / done, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": w.ncell, "velocities": w.nv,
+                       "tables": "the reference's own mesh and velocity tables of the workload "
+                                 "(tests/golden/workload_config2.npz)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{done} timed steps (requested {args.steps}, at most 200) of the full "
+                                       f"workload after {warm} warm-up step(s), {threads} threads"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 def run_other_configs(tmp: str) -> dict:
@@ -349,14 +356,18 @@ def run_batched(tmp: str, steps: int = 20, warm: int = 3, autotune: bool = True)
     tune_s = time.perf_counter() - t0
     # the same instances stepped one at a time, each with its tuned shape (device time per step, summed)
     alone_ms = 0.0
-    for path in paths:
+    alone_by_dvs, cx_by_dvs = {}, {}
+    for inst, path in zip(insts, paths):
         case = mg.Case(path)
         rho, u, T, mask = case.initial_fields()
         s = mg.Solver(case=case, precision=mg.FP32, mask=mask)
         s.init_macros(rho, u, T, None, 0)
         s.step(1)
         s.step(3)
-        alone_ms += s.last_step_ms() / 3
+        ms1 = s.last_step_ms() / 3
+        alone_ms += ms1
+        alone_by_dvs[inst["dvs"]] = alone_by_dvs.get(inst["dvs"], 0.0) + ms1
+        cx_by_dvs[inst["dvs"]] = cx_by_dvs.get(inst["dvs"], 0) + case.ncell * case.nv
         s.close()
         case.close()
     # batch members: the tuned tile size and velocities per lane, one velocity group per tile (the
@@ -395,33 +406,25 @@ def run_batched(tmp: str, steps: int = 20, warm: int = 3, autotune: bool = True)
             "value": cx / (ms * 1e-3), "unit": UNIT, "steps": steps, "ms_per_step": ms / steps,
             "cell_xi_per_step": cx_step, "device_bytes": dev_bytes, "graph_launches_per_step": launches / steps,
             "alone_ms_per_step_sum": alone_ms, "batch_over_alone": alone_ms / (ms / steps),
+            "alone_by_dvs": {d: {"members": sum(1 for i in insts if i["dvs"] == d), "ms_per_step_sum": alone_by_dvs[d],
+                                 "cell_xi_per_step": cx_by_dvs[d],
+                                 "cell_xi_per_s": cx_by_dvs[d] / (alone_by_dvs[d] * 1e-3)} for d in alone_by_dvs},
+            "batch_hbm_frac": 16.0 * cx / (ms * 1e-3) / 1e9 / measured_peak_hbm()[0],
             "members_stopped": stopped, "setup_seconds": setup_s, "autotune_seconds": tune_s,
             "tuned_shapes": {f"{k[0]}^2 {k[1]}": v for k, v in tuned.items()}}
 
 
-def run_served(tmp: str, count: int = 200, rate: float = 20.0, max_step: int = 8000, poll_steps: int = 100,
-               members: int = 64) -> dict:
-    """Config 5: a seeded Poisson stream of cavity solves, each run to convergence on U, served with
-    continuous batching; time-to-converged per request (submit to retirement)."""
-    import cases
+def _serve(reqs, paths, params, members: int, poll_steps: int) -> tuple[list[dict], float, tuple]:
+    """Submits each request at its arrival time to a server with continuous batching and polls until
+    every solve has retired; per request (in submission order): steps, converged, NaN cells, seconds
+    from submission to retirement."""
     import meso_gpu as mg
 
-    reqs = cases.config5_requests(count=count, rate=rate)
-    paths, params = [], []
-    for r in reqs:
-        p = cases.config5_case(os.path.join(tmp, f"s{r['index']}"), r, max_step)
-        prm = mg.Case(p).params
-        prm.residual_interval = 100
-        prm.residual_limit = 1e-6
-        prm.residual_fields = mg.RES_U | mg.RES_L2
-        paths.append(p)
-        params.append(prm)
     rt = _cudart()
     free_b, total_b = ctypes.c_size_t(), ctypes.c_size_t()
     rt.cudaMemGetInfo(ctypes.byref(free_b), ctypes.byref(total_b))
     srv = mg.Server(hbm_budget_bytes=int(free_b.value * 0.8), max_members=members)
-    done = {}
-    i = 0
+    done, i, count = {}, 0, len(reqs)
     t0 = time.perf_counter()
     while len(done) < count:
         now = time.perf_counter() - t0
@@ -434,38 +437,105 @@ def run_served(tmp: str, count: int = 200, rate: float = 20.0, max_step: int = 8
             continue
         for t in srv.poll(poll_steps):
             _, st, sec = srv.result(t)
-            done[t] = (st.step, st.converged, st.run_state, sec[0], sec[1])
+            done[t] = dict(step=st.step, converged=st.converged, bad=st.bad_cells, latency=sec[0])
             srv.release(t)
     wall = time.perf_counter() - t0
-    gpu_ms, poll_ms, batch_steps = srv.stats()
+    stats = srv.stats()
     srv.close()
-    lat = sorted(v[3] for v in done.values())
-    steps = [v[0] for v in done.values()]
-    conv = sum(v[1] for v in done.values())
-    # serial plain FP64: FP64 step time of each request class x the steps each solve took
-    cls_ms = {}
-    for r, p in zip(reqs, paths):
-        key = (r["side"], r["dvs"])
-        if key in cls_ms:
-            continue
-        case = mg.Case(p)
+    return [done[k] for k in sorted(done)], wall, stats  # tags follow submission order
+
+
+def _serial_fp64(reqs, paths, params, res, sample: list[int], max_step: int, poll_steps: int,
+                 budget_s: float) -> list[dict]:
+    """The sampled requests run one at a time in plain FP64 with the same stopping rule, timed on the
+    host (wall time of the steps), each within a wall-time budget."""
+    import meso_gpu as mg
+
+    out = []
+    for k in sample:
+        case = mg.Case(paths[k])
         rho, u, T, mask = case.initial_fields()
-        s = mg.Solver(case=case, precision=mg.FP64, mask=mask)
+        prm = params[k]
+        prm.precision = mg.FP64
+        s = mg.Solver(case=case, precision=mg.FP64, mask=mask, params=prm)
         s.init_macros(rho, u, T, None, 0)
-        s.step(2)
-        s.step(10)
-        cls_ms[key] = s.last_step_ms() / 10
+        t1 = time.perf_counter()
+        n, within = 0, True
+        try:
+            while n < max_step:
+                if time.perf_counter() - t1 > budget_s:
+                    within = False
+                    break
+                got = s.step(min(poll_steps, max_step - n))
+                n += got
+                if got == 0 or s.status().run_state == 0:
+                    break
+        except mg.MesoError:
+            pass
+        secs = time.perf_counter() - t1
+        st = s.status()
         s.close()
-    serial_s = sum(cls_ms[(r["side"], r["dvs"])] * 1e-3 * v[0] for r, v in zip(reqs, (done[k] for k in sorted(done))))
-    q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))]
+        case.close()
+        out.append({"request": k, "cells": reqs[k]["side"] ** 2, "dvs": reqs[k]["dvs"], "steps": st.step,
+                    "converged": st.converged, "finished_within_budget": within, "seconds": secs,
+                    "served_seconds": res[k]["latency"], "served_steps": res[k]["step"]})
+    return out
+
+
+def _served_summary(reqs, res, wall: float, stats: tuple, fp64: list[dict]) -> dict:
+    conv = [r for r in res if r["converged"]]
+    lat = sorted(r["latency"] for r in conv)
+    q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))] if lat else None
+    gpu_ms, poll_ms, batch_steps = stats
+    fin = [x for x in fp64 if x["finished_within_budget"]]
+    return {"solves_per_s": len(res) / wall, "wall_seconds": wall, "batch_steps": batch_steps,
+            "gpu_seconds": gpu_ms * 1e-3, "poll_host_seconds": (poll_ms - gpu_ms) * 1e-3,
+            "converged": len(conv), "capped": sum(1 for r in res if not r["converged"] and r["bad"] == 0),
+            "failed_nan": sum(1 for r in res if not r["converged"] and r["bad"] > 0),
+            "p50_s_converged": q(0.50), "p99_s_converged": q(0.99),
+            "mean_steps_converged": float(np.mean([r["step"] for r in conv])) if conv else None,
+            "by_dvs": {d: {"requests": sum(1 for r in reqs if r["dvs"] == d),
+                           "converged": sum(1 for r, x in zip(reqs, res) if r["dvs"] == d and x["converged"])}
+                       for d in sorted({r["dvs"] for r in reqs})},
+            "serial_fp64_sample": fp64,
+            "serial_fp64_solves_per_s_sample": (len(fin) / sum(x["seconds"] for x in fin)) if fin else None,
+            "served_solves_per_s_same_sample": (len(fin) / sum(x["served_seconds"] for x in fin)) if fin else None,
+            "serial_fp64_note": "measured: the sampled requests run one at a time in plain FP64, same stopping rule"}
+
+
+def _requests(tmp, tag, reqs, max_step, nc_points):
+    import cases
+    import meso_gpu as mg
+
+    paths, params = [], []
+    for r in reqs:
+        p = cases.config5_case(os.path.join(tmp, f"{tag}{r['index']}"), r, max_step, nc_points=nc_points)
+        prm = mg.Case(p).params
+        prm.residual_interval = 100
+        prm.residual_limit = 1e-6
+        prm.residual_fields = mg.RES_U | mg.RES_L2
+        paths.append(p)
+        params.append(prm)
+    return paths, params
+
+
+def run_served(tmp: str, count: int = 200, rate: float = 20.0, max_step: int = 8000, poll_steps: int = 100,
+               members: int = 64, fp64_sample: int = 6, fp64_budget_s: float = 20.0) -> dict:
+    """Config 5 scaled to a bench run: a seeded Poisson stream of small cavity solves, each run to
+    convergence on U, served with continuous batching; time-to-converged per request (submission to
+    retirement) over the solves that converged, capped and failed solves counted apart; serial plain
+    FP64 measured on a seeded sample of the requests."""
+    import cases
+
+    reqs = cases.config5_requests(count=count, rate=rate)
+    paths, params = _requests(tmp, "s", reqs, max_step, 21)
+    res, wall, stats = _serve(reqs, paths, params, members, poll_steps)
+    sample = sorted(int(x) for x in np.random.default_rng(5).choice(count, size=min(fp64_sample, count), replace=False))
+    fp64 = _serial_fp64(reqs, paths, params, res, sample, max_step, poll_steps, fp64_budget_s)
     return {"workload": f"{count} cavity solves, Poisson arrivals {rate}/s (seed 2), sides {{16,24,32}} quads, "
                         "log10 Kn ~ U(-2,0), DVS {hGH 28x28, NC 21x21}, lid ~ U(0.05,0.15), FP32 storage, "
                         f"run to L2-relative residual 1e-6 on U per 100 steps (max-step {max_step})",
-            "max_members": members, "solves_per_s": count / wall, "wall_seconds": wall,
-            "batch_steps": batch_steps, "gpu_seconds": gpu_ms * 1e-3, "poll_host_seconds": (poll_ms - gpu_ms) * 1e-3, "p50_s": q(0.50), "p99_s": q(0.99),
-            "converged": conv, "reached_max_step_or_failed": count - conv, "mean_steps": float(np.mean(steps)),
-            "serial_fp64_solves_per_s_est": count / serial_s if serial_s > 0 else None,
-            "serial_fp64_note": "FP64 step time of each request class x the steps each solve took, summed"}
+            "max_members": members, **_served_summary(reqs, res, wall, stats, fp64)}
 
 
 def run_profile(args) -> int:
@@ -520,105 +590,22 @@ def run_profile(args) -> int:
 
 
 def run_served_config5(tmp: str, count: int = 40, rate: float = 20.0, max_step: int = 3000, poll_steps: int = 100,
-                       members: int = 64, fp64_sample: int = 3, fp64_budget_s: float = 30.0) -> dict:
+                       members: int = 64, fp64_sample: int = 3, fp64_budget_s: float = 20.0) -> dict:
     """The served stream drawn from the batch workload's distribution (sides {32,48,64,96,128} quads,
     DVS {D2Q9, hGH 28^2, NC 101^2}, log10 Kn ~ U(-2,0), lid ~ U(.05,.15)), Poisson arrivals at 20/s
-    (seed 2), bounded to `count` requests and `max_step` steps each.  Time-to-converged over the
-    solves that converged; capped and failed (NaN) solves counted apart.  Serial plain FP64 is measured
-    (not estimated) on a seeded sample of the requests, each run alone to the same stopping rule,
-    within a wall-time budget."""
+    (seed 2), bounded to `count` requests and `max_step` steps each, reported like run_served."""
     import cases
-    import meso_gpu as mg
 
     reqs = cases.config5_requests(count=count, rate=rate, sides=(32, 48, 64, 96, 128), dvs_kinds=("d2q9", "hgh", "nc"))
-    paths, params = [], []
-    for r in reqs:
-        p = cases.config5_case(os.path.join(tmp, f"c5_{r['index']}"), r, max_step, nc_points=101)
-        prm = mg.Case(p).params
-        prm.residual_interval = 100
-        prm.residual_limit = 1e-6
-        prm.residual_fields = mg.RES_U | mg.RES_L2
-        paths.append(p)
-        params.append(prm)
-    rt = _cudart()
-    free_b, total_b = ctypes.c_size_t(), ctypes.c_size_t()
-    rt.cudaMemGetInfo(ctypes.byref(free_b), ctypes.byref(total_b))
-    srv = mg.Server(hbm_budget_bytes=int(free_b.value * 0.8), max_members=members)
-    done = {}
-    i = 0
-    t0 = time.perf_counter()
-    while len(done) < count:
-        now = time.perf_counter() - t0
-        while i < count and reqs[i]["arrival"] <= now:
-            srv.submit(paths[i], params[i])
-            i += 1
-        pend, run, _ = srv.counts()
-        if pend + run == 0:
-            time.sleep(max(0.0, min(0.01, reqs[i]["arrival"] - now)) if i < count else 0.0)
-            continue
-        for t in srv.poll(poll_steps):
-            _, st, sec = srv.result(t)
-            done[t] = dict(step=st.step, converged=st.converged, run_state=st.run_state, bad=st.bad_cells,
-                           latency=sec[0])
-            srv.release(t)
-    wall = time.perf_counter() - t0
-    gpu_ms, poll_ms, batch_steps = srv.stats()
-    srv.close()
-    res = [done[k] for k in sorted(done)]  # tags follow submission order
-    conv = [r for r in res if r["converged"]]
-    failed = [r for r in res if not r["converged"] and r["bad"] > 0]
-    capped = [r for r in res if not r["converged"] and r["bad"] == 0]
-    lat = sorted(r["latency"] for r in conv)
-    q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))] if lat else None
-    # serial plain FP64 on a seeded sample, each alone, the same stopping rule
-    rng = np.random.default_rng(5)
-    sample = sorted(int(x) for x in rng.choice(count, size=min(fp64_sample, count), replace=False))
-    fp64 = []
-    t_budget = time.perf_counter()
-    for k in sample:
-        if time.perf_counter() - t_budget > fp64_budget_s:
-            fp64.append({"request": k, "skipped": "over the wall-time budget"})
-            continue
-        case = mg.Case(paths[k])
-        rho, u, T, mask = case.initial_fields()
-        prm = params[k]
-        prm.precision = mg.FP64
-        s = mg.Solver(case=case, precision=mg.FP64, mask=mask, params=prm)
-        s.init_macros(rho, u, T, None, 0)
-        t1 = time.perf_counter()
-        n = 0
-        try:
-            while n < max_step and time.perf_counter() - t1 < fp64_budget_s:
-                got = s.step(min(poll_steps, max_step - n))
-                n += got
-                if got == 0 or s.status().run_state == 0:
-                    break
-        except mg.MesoError:
-            pass
-        secs = time.perf_counter() - t1
-        st = s.status()
-        s.close()
-        case.close()
-        fp64.append({"request": k, "cells": reqs[k]["side"] ** 2, "dvs": reqs[k]["dvs"], "steps": st.step,
-                     "converged": st.converged, "seconds": secs,
-                     "served_seconds": res[k]["latency"], "served_steps": res[k]["step"]})
-    timed = [x for x in fp64 if "seconds" in x]
+    paths, params = _requests(tmp, "c5_", reqs, max_step, 101)
+    res, wall, stats = _serve(reqs, paths, params, members, poll_steps)
+    sample = sorted(int(x) for x in np.random.default_rng(5).choice(count, size=min(fp64_sample, count), replace=False))
+    fp64 = _serial_fp64(reqs, paths, params, res, sample, max_step, poll_steps, fp64_budget_s)
     return {"workload": f"{count} cavity solves drawn like the batch workload: sides {{32,48,64,96,128}} quads, "
                         "log10 Kn ~ U(-2,0), DVS {D2Q9, hGH 28x28, NC 101x101}, lid ~ U(0.05,0.15), Poisson arrivals "
                         f"{rate}/s (seed 2), FP32 storage, run to L2-relative residual 1e-6 on U per 100 steps, "
                         f"at most {max_step} steps",
-            "max_members": members, "solves_per_s": count / wall, "wall_seconds": wall, "batch_steps": batch_steps,
-            "gpu_seconds": gpu_ms * 1e-3, "converged": len(conv), "capped": len(capped), "failed_nan": len(failed),
-            "p50_s_converged": q(0.50), "p99_s_converged": q(0.99),
-            "mean_steps_converged": float(np.mean([r["step"] for r in conv])) if conv else None,
-            "by_dvs": {d: {"converged": sum(1 for r, x in zip(reqs, res) if r["dvs"] == d and x["converged"]),
-                           "capped": sum(1 for r, x in zip(reqs, res) if r["dvs"] == d and not x["converged"]
-                                         and x["bad"] == 0),
-                           "failed_nan": sum(1 for r, x in zip(reqs, res) if r["dvs"] == d and x["bad"] > 0)}
-                       for d in ("d2q9", "hgh", "nc")},
-            "serial_fp64_sample": fp64,
-            "serial_fp64_solves_per_s_sample": (len(timed) / sum(x["seconds"] for x in timed)) if timed else None,
-            "served_solves_per_s_same_sample": (len(timed) / sum(x["served_seconds"] for x in timed)) if timed else None}
+            "max_members": members, **_served_summary(reqs, res, wall, stats, fp64)}
 
 
 def main() -> int:
@@ -776,7 +763,7 @@ def main() -> int:
             "gpu_launches": launches,
         }
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(path, 12.0, os.cpu_count() or 1)
+            line["cpu_baseline"] = cpu_baseline(12.0, os.cpu_count() or 1)
         if not args.no_batched:
             line["other_configs"] = run_other_configs(tmp)
             line["batched"] = run_batched(tmp)

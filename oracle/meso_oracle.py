@@ -57,6 +57,139 @@ def _p(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+# The C ABI's descriptor layouts (include/meso_gpu.h), so that the oracle can be fed without the
+# product library: meso_mesh_desc, meso_dvs_desc, meso_mark_desc, meso_params.
+_dp, _ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("ncell", C.c_int32), ("nface", C.c_int32),
+                ("cell_pos", _dp), ("cell_vol", _dp), ("cell_group", _ip),
+                ("cell_face_ptr", _ip), ("cell_face", _ip), ("cell_nbr_ptr", _ip), ("cell_nbr", _ip),
+                ("lsq_w", _dp), ("lsq_dr", _dp), ("lsq_c", _dp),
+                ("face_cell", _ip), ("face_pos", _dp), ("face_area", _dp), ("face_normal", _dp),
+                ("face_mark", _ip), ("min_cell_size", C.c_double), ("total_volume", C.c_double)]
+
+
+class DvsDesc(C.Structure):
+    _fields_ = [("nv", C.c_int32), ("xi", _dp), ("w", _dp), ("sym", _ip), ("tensor_n", C.c_int32),
+                ("axis", _dp), ("max_magnitude", C.c_double)]
+
+
+class MarkDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("temperature_type", C.c_int32), ("direction", C.c_int32),
+                ("pad_", C.c_int32), ("density", C.c_double), ("temperature", C.c_double),
+                ("pressure", C.c_double), ("velocity", C.c_double * 3), ("alpha_u", C.c_double),
+                ("alpha_T", C.c_double)]
+
+
+class Params(C.Structure):
+    _fields_ = [("solver", C.c_int32), ("precision", C.c_int32), ("gradient_switch", C.c_int32),
+                ("limiter_switch", C.c_int32), ("K", C.c_int32), ("residual_interval", C.c_int32),
+                ("dt", C.c_double), ("R", C.c_double), ("T0", C.c_double), ("rho0", C.c_double),
+                ("L0", C.c_double), ("mu0", C.c_double), ("vhs_index", C.c_double), ("Pr", C.c_double),
+                ("Ma", C.c_double), ("Re", C.c_double), ("CFL", C.c_double), ("venkata_k", C.c_double),
+                ("residual_limit", C.c_double), ("residual_fields", C.c_int32), ("tile_cells", C.c_int32),
+                ("vpl", C.c_int32), ("ngroup", C.c_int32), ("pad_", C.c_int32)]
+
+
+_BC = {"fluid-interior": 0, "farfield-inlet": 1, "pressure-inlet": 2, "freestream-inlet": 3, "farfield-outlet": 4,
+       "pressure-outlet": 5, "wall": 6, "slip-wall": 7, "symmetry": 8}  # config.cpp:5-15
+_PATCH = {"zeroGradient": 0, "fixedValue": 1, "calculated": 2, "fromFile": 3, "switch": 4}
+
+
+def _case_blocks(text: str):
+    """[settings] key/value pairs and the [group] / [mark] blocks of a case file (config.cpp:30-108):
+    each block a dict of key -> tokens."""
+    settings, blocks, cur = {}, [], None
+    for line in text.splitlines():
+        t = line.split()
+        if not t or t[0] == "#":
+            continue
+        if t[0] == "[settings]":
+            cur = None
+        elif t[0] in ("[group]", "[mark]"):
+            cur = {"kind": t[0][1:-1]}
+            blocks.append(cur)
+        elif cur is None:
+            settings[t[0]] = t[1] if len(t) > 1 else ""
+        else:
+            cur[t[0]] = t[1:]
+    return settings, blocks
+
+
+class Workload:
+    """A Shakhov case from the reference's own mesh and velocity tables (tests/golden/
+    workload_config2.npz, written by the reference's constructor) and its case file text: the
+    descriptors the oracle takes, built without the product library.  Covers what the rarefied-cavity
+    workload uses: fixedValue group patches and wall marks with fixedValue velocity / temperature."""
+
+    def __init__(self, npz_path: str):
+        z = np.load(npz_path)
+        self._a = {k: (np.ascontiguousarray(z[k]) if z[k].ndim else z[k][()]) for k in z.files
+                   if k not in ("case_text", "face_names")}
+        a = self._a
+        settings, blocks = _case_blocks(str(z["case_text"]))
+        if settings.get("solver") != "cdugks@shakhov":
+            raise NotImplementedError("Workload covers the Shakhov solver")
+        m = MeshDesc()
+        m.dim, m.ncell, m.nface = int(a["dim"]), int(a["ncell"]), int(a["nface"])
+        for k in ("cell_pos", "cell_vol", "lsq_w", "lsq_dr", "lsq_c", "face_pos", "face_area", "face_normal"):
+            setattr(m, k, a[k].ctypes.data_as(_dp))
+        a["face_mark"] = a["face_group"]
+        for k in ("cell_group", "cell_face_ptr", "cell_face", "cell_nbr_ptr", "cell_nbr", "face_cell", "face_mark"):
+            setattr(m, k, a[k].ctypes.data_as(_ip))
+        m.min_cell_size, m.total_volume = float(a["min_cell_size"]), float(a["total_volume"])
+        self.mesh = m
+        d = DvsDesc()
+        d.nv = int(a["w"].size)
+        d.xi, d.w, d.sym = a["xi"].ctypes.data_as(_dp), a["w"].ctypes.data_as(_dp), a["sym"].ctypes.data_as(_ip)
+        d.tensor_n, d.axis, d.max_magnitude = 0, None, float(a["dvs_max_magnitude"])
+        self.dvs = d
+        marks = {b["name"][0]: b for b in blocks if b["kind"] == "mark"}
+        names = [str(x) for x in z["face_names"]]
+        self._marks = (MarkDesc * len(names))()
+        for g, name in enumerate(names):
+            md = self._marks[g]
+            if name == "fluid-interior":
+                continue
+            b = marks[name]
+            md.type = _BC[b["type"][0]]
+            if md.type != _BC["wall"]:
+                raise NotImplementedError("Workload covers wall marks")
+            if "velocity" in b:
+                for k in range(3):
+                    md.velocity[k] = float(b["velocity"][2 + k])
+            if "temperature" in b:
+                md.temperature_type = _PATCH[b["temperature"][0]]
+                md.temperature = float(b["temperature"][2])
+        self.marks_ptr = C.cast(self._marks, C.POINTER(MarkDesc))
+        self.nmarks = len(names)
+        get = lambda k, dflt: float(settings.get(k, dflt))
+        p = Params()
+        p.solver, p.precision = 2, 0
+        p.gradient_switch = 1 if settings.get("gradient-switch", "True") == "True" else 0
+        p.limiter_switch = 1 if settings.get("limiter-switch", "False") == "True" else 0
+        p.K, p.residual_interval = int(settings.get("gas-k", "0")), 100
+        p.dt, p.R, p.T0 = get("timeStep", 1e-5), get("gas-constant", 0.5), get("ref-temperature", 1.0)
+        p.rho0, p.L0, p.mu0 = get("ref-density", 1.0), get("ref-length", 1.0), get("ref-viscosity", 1.6e-5)
+        p.vhs_index, p.Pr, p.residual_limit = get("vhs-index", 0.81), get("Pr", 0.67), get("residual-limit", 1e-6)
+        self.params = p
+        # initial fields from the one cell group (fixedValue density / temperature / velocity)
+        groups = [b for b in blocks if b["kind"] == "group"]
+        if len(groups) != 1:
+            raise NotImplementedError("Workload covers one cell group")
+        gb = groups[0]
+        n = m.ncell
+        val = lambda key: float(gb[key][2]) if key in gb else 0.0
+        self.rho = np.full(n, val("density"))
+        self.T = np.full(n, val("temperature"))
+        self.u = np.zeros((n, 3))
+        if "velocity" in gb:
+            self.u[:] = [float(x) for x in gb["velocity"][2:5]]
+        self.ncell, self.nv = n, d.nv
+
+
 class Oracle:
     def __init__(self, case, nthreads: int = 1, mask: np.ndarray | None = None, params=None):
         h = C.c_void_p()

@@ -7,7 +7,10 @@
 // then writes the macroscopic cell fields (and optionally the mesh/DVS tables
 // the solver built) as raw little-endian binary for the parity tests.
 //
-//   meso_ref <case-file> <nsteps> <out.bin> [--mesh <mesh.bin>] [--every K] [--output 1]
+//   meso_ref <case-file> <nsteps> <out.bin> [--mesh <mesh.bin>] [--every K] [--output 1] [--mesh-only 1]
+//
+// --mesh-only 1 writes the mesh/DVS tables (--mesh) after the solver's constructor and exits
+// before initial() allocates the distribution functions.
 //
 // --output 1 calls the solver's own output() after initial() and after the
 // last step, as handle_solver does (exec.cpp:150-164): grid.plt, step-N/
@@ -105,9 +108,10 @@ void write_mesh(const std::string &path, MESO::fvmMesh::Mesh &m, MESO::fvmMesh::
 
 template <class S>
 int run(MESO::ArgParser &parser, MESO::Solver::Config &config, int nsteps, const std::string &out,
-        const std::string &mesh_out, int every, int output) {
+        const std::string &mesh_out, int every, int output, int mesh_only) {
     S s(parser, config);
     if (!mesh_out.empty()) write_mesh(mesh_out, s.mesh, s.dvs_mesh);
+    if (mesh_only) return 0;
     s.initial();
     if (output) s.output();
     auto t0 = std::chrono::steady_clock::now();
@@ -145,12 +149,13 @@ int main(int argc, char **argv) {
     int nsteps = std::atoi(argv[2]);
     std::string out = argv[3];
     std::string mesh_out;
-    int every = 0, output = 0;
+    int every = 0, output = 0, mesh_only = 0;
     for (int i = 4; i + 1 < argc; i += 2) {
         std::string k = argv[i];
         if (k == "--mesh") mesh_out = argv[i + 1];
         else if (k == "--every") every = std::atoi(argv[i + 1]);
         else if (k == "--output") output = std::atoi(argv[i + 1]);
+        else if (k == "--mesh-only") mesh_only = std::atoi(argv[i + 1]);
     }
     char a0[] = "meso_ref", a1[] = "--case";
     std::vector<char> a2(case_file.begin(), case_file.end());
@@ -165,11 +170,11 @@ int main(int argc, char **argv) {
     int rc = 3;
     try {
         if (solver == "dugks@incompressible")
-            rc = run<MESO::Solver::DUGKS>(parser, config, nsteps, out, mesh_out, every, output);
+            rc = run<MESO::Solver::DUGKS>(parser, config, nsteps, out, mesh_out, every, output, mesh_only);
         else if (solver == "cdugks@incompressible")
-            rc = run<MESO::Solver::CDUGKS>(parser, config, nsteps, out, mesh_out, every, output);
+            rc = run<MESO::Solver::CDUGKS>(parser, config, nsteps, out, mesh_out, every, output, mesh_only);
         else if (solver == "cdugks@shakhov")
-            rc = run<MESO::Solver::CDUGKS_SHAKHOV>(parser, config, nsteps, out, mesh_out, every, output);
+            rc = run<MESO::Solver::CDUGKS_SHAKHOV>(parser, config, nsteps, out, mesh_out, every, output, mesh_only);
         else
             std::fprintf(stderr, "unknown solver %s\n", solver.c_str());
     } catch (const std::exception &e) {

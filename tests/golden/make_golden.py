@@ -15,6 +15,9 @@ macroscopic fields (rho, u, T, q), step count, run_state and solution time in
 (geometry_<name>.npz).  The inputs are committed so the fixtures do not depend
 on the scipy / numpy versions that generated them.
 
+The rarefied-cavity workload's tables as the reference builds them go to
+workload_config2.npz (make_workload).
+
 Further cases:
   * ref_*: the reference's own shipped inputs (files/cavity.neu with
     case-re400.txt, case-re1000.txt and case-kn0.075.txt and their velocity
@@ -178,6 +181,87 @@ def read_mesh(path: str) -> dict:
                 sym=np.array(sym, np.int32), dvs_max_magnitude=vmax)
 
 
+def read_mesh_full(path: str) -> dict:
+    """Every table the harness's --mesh dump holds, as flat arrays in the layout of the C ABI's
+    mesh and velocity-set descriptors (cells and faces in the reference's order)."""
+    b = open(path, "rb").read()
+    o = [0]
+
+    def take(fmt):
+        v = struct.unpack_from("<" + fmt, b, o[0])
+        o[0] += struct.calcsize("<" + fmt)
+        return v if len(v) > 1 else v[0]
+
+    assert take("i") == 0x4D455348
+    dim, C, F, N = take("4i")
+    mcs, tv = take("2d")
+    pos, vol, grp, cf_ptr, cf, nb_ptr, nbr, w, dr, lsq_c = [], [], [], [0], [], [0], [], [], [], []
+    for _ in range(C):
+        _, g = take("2i")
+        grp.append(g)
+        pos.append(take("3d"))
+        vol.append(take("d"))
+        nf = take("i")
+        ids = take(f"{nf}i")
+        cf.extend(ids if nf > 1 else [ids])
+        cf_ptr.append(len(cf))
+        nn = take("i")
+        for _ in range(nn):
+            nbr.append(take("i"))
+            w.append(take("d"))
+            dr.append(take("3d"))
+        nb_ptr.append(len(nbr))
+        lsq_c.append(take("9d"))
+    fc, fgrp, fpos, area, n0 = [], [], [], [], []
+    for _ in range(F):
+        fc.append(take("2i"))
+        fgrp.append(take("i"))
+        fpos.append(take("3d"))
+        area.append(take("d"))
+        n0.append(take("3d"))
+        take("3d")
+    nv = take("i")
+    vmax = take("d")
+    xi, wv, sym = [], [], []
+    for _ in range(nv):
+        xi.append(take("3d"))
+        wv.append(take("d"))
+        sym.append(take("3i"))
+    i32 = lambda a: np.asarray(a, np.int32)
+    f64 = lambda a: np.asarray(a, np.float64)
+    return dict(dim=dim, ncell=C, nface=F, nnode=N, min_cell_size=mcs, total_volume=tv,
+                cell_pos=f64(pos).reshape(-1), cell_vol=f64(vol), cell_group=i32(grp), cell_face_ptr=i32(cf_ptr),
+                cell_face=i32(cf), cell_nbr_ptr=i32(nb_ptr), cell_nbr=i32(nbr), lsq_w=f64(w),
+                lsq_dr=f64(dr).reshape(-1), lsq_c=f64(lsq_c).reshape(-1), face_cell=i32(fc).reshape(-1),
+                face_group=i32(fgrp), face_pos=f64(fpos).reshape(-1), face_area=f64(area),
+                face_normal=f64(n0).reshape(-1), xi=f64(xi).reshape(-1), w=f64(wv), sym=i32(sym).reshape(-1),
+                dvs_max_magnitude=vmax)
+
+
+def make_workload() -> None:
+    """tests/golden/workload_config2.npz: the rarefied-cavity workload's mesh and velocity tables as
+    the reference itself builds them (its constructor, --mesh-only), with the case file text and the
+    mesh's face-group names; the CPU reference arm of bench.py runs the oracle on them."""
+    import tempfile
+
+    with tempfile.TemporaryDirectory() as d:
+        path = cases.config2(os.path.join(d, "c2"), 500, "fp64")
+        cd = os.path.dirname(path)
+        r = subprocess.run([REF, os.path.basename(path), "0", "out.bin", "--mesh", "mesh.bin", "--mesh-only", "1"],
+                           cwd=cd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise SystemExit(f"workload: reference failed: {r.stderr}")
+        m = read_mesh_full(os.path.join(cd, "mesh.bin"))
+        names = ["fluid-interior"]
+        lines = open(os.path.join(cd, "mesh.neu")).read().splitlines()
+        for i, line in enumerate(lines):
+            if line.split()[:2] == ["BOUNDARY", "CONDITIONS"]:
+                names.append(lines[i + 1].split()[0])
+        np.savez_compressed(os.path.join(HERE, "workload_config2.npz"), case_text=open(path).read(),
+                            face_names=np.array(names), **m)
+    print(f"workload_config2: {m['ncell']} cells, {m['nface']} faces, {len(m['w'])} velocities")
+
+
 def _case_name(case_path: str) -> str:
     for line in open(case_path):
         t = line.split()
@@ -207,6 +291,8 @@ def main() -> None:
         sys.exit("oracle/_ref/meso_ref missing: run oracle/build_ref.sh first")
     os.makedirs(CASE_DIR, exist_ok=True)
     only = set(sys.argv[1:])
+    if not only or "workload_config2" in only:
+        make_workload()
     for name, (build, steps) in GOLDEN.items():
         if only and name not in only:
             continue

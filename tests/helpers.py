@@ -63,7 +63,9 @@ HEAVY_GOLDENS = ("config3_cfl08_blowup", "tri64_nc21_blowup")
 
 
 def golden_names() -> list[str]:
-    return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz") and not f.startswith("geometry_"))
+    """The step goldens (the reference's fields after N steps; geometry_* and workload_* hold tables)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR)
+                  if f.endswith(".npz") and not f.startswith(("geometry_", "workload_")))
 
 
 def golden_case(name: str) -> str:
