@@ -336,6 +336,42 @@ def run_other_configs(tmp: str) -> dict:
     return out
 
 
+def run_host_pipeline(tmp: str, repeats: int = 5) -> dict:
+    """Admission cost of a solve on the host: case load (case file, Gambit mesh, faces, geometry,
+    least squares, velocity set, flattening), context creation (renumbering, tile plan, device
+    tables) and the initial state, for the rarefied workload and a 128^2 hGH 28^2 served-size
+    cavity; medians of `repeats` runs, wall time."""
+    import cases
+    import meso_gpu as mg
+
+    out = {}
+    paths = {"config2_7744_nc101": cases.config2(os.path.join(tmp, "hp_c2"), 500, "fp32"),
+             "quad128_hgh28": cases.shakhov_cavity(os.path.join(tmp, "hp_q128"), "quad", 128, "hgh", 28, 0.1, 0.15,
+                                                   100, name="q128", precision="fp32")}
+    rt = _cudart()
+    for name, p in paths.items():
+        t_load, t_ctx, t_init = [], [], []
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            case = mg.Case(p)
+            t1 = time.perf_counter()
+            rho, u, T, mask = case.initial_fields()
+            s = mg.Solver(case=case, precision=mg.FP32, mask=mask)
+            rt.cudaDeviceSynchronize()
+            t2 = time.perf_counter()
+            s.init_macros(rho, u, T, None, 0)
+            rt.cudaDeviceSynchronize()
+            t3 = time.perf_counter()
+            s.close()
+            case.close()
+            t_load.append((t1 - t0) * 1e3)
+            t_ctx.append((t2 - t1) * 1e3)
+            t_init.append((t3 - t2) * 1e3)
+        out[name] = {"case_load_ms": statistics.median(t_load), "context_ms": statistics.median(t_ctx),
+                     "initial_state_ms": statistics.median(t_init)}
+    return out
+
+
 def run_batched(tmp: str, steps: int = 20, warm: int = 3, autotune: bool = True) -> dict:
     """Config 4: 64 cavity instances (seeded draws of mesh side, Kn, velocity set, lid) in one batch."""
     import cases
@@ -765,6 +801,7 @@ def main() -> int:
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(12.0, os.cpu_count() or 1)
         if not args.no_batched:
+            line["host_pipeline"] = run_host_pipeline(tmp)
             line["other_configs"] = run_other_configs(tmp)
             line["batched"] = run_batched(tmp)
         if not args.no_served:
