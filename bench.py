@@ -721,6 +721,8 @@ def main() -> int:
         # ---- plain FP64 step on the same workload, run for the workload's 500 steps (K64 of them
         # timed), and the FP32 form's error against it there; the FP64 fields' own change over the
         # last 100 steps shows how far from steady state step 500 is
+        # (under torchrun, N > 1, only the timed FP64 steps: the rest holds every GPU for a minute)
+        extras = world == 1
         K64 = max(3, min(K, 50))
         nerr = 500
         s64 = mg.Solver(case=case, precision=mg.FP64, mask=mask)
@@ -729,18 +731,20 @@ def main() -> int:
         s64.step(K64)
         ms64 = s64.last_step_ms()
         fp64_value = cx * K64 / (ms64 * 1e-3)
-        s64.step(nerr - 100 - 1 - K64)
-        b400 = s64.macros(C)
-        s64.step(100)
-        b = s64.macros(C)
+        err = None
+        if extras:
+            s64.step(nerr - 100 - 1 - K64)
+            b400 = s64.macros(C)
+            s64.step(100)
+            b = s64.macros(C)
+            s32 = mg.Solver(case=case, precision=mg.FP32, mask=mask)
+            s32.init_macros(rho, u, T, None, 0)
+            s32.step(nerr)
+            a = s32.macros(C)
+            s32.close()
+            err = {k: relerr(x, y) for k, x, y in zip(("rho", "u", "T", "q"), a, b)}
+            err["fp64_change_steps_400_500"] = {k: relerr(x, y) for k, x, y in zip(("rho", "u", "T", "q"), b400, b)}
         s64.close()
-        s32 = mg.Solver(case=case, precision=mg.FP32, mask=mask)
-        s32.init_macros(rho, u, T, None, 0)
-        s32.step(nerr)
-        a = s32.macros(C)
-        s32.close()
-        err = {k: relerr(x, y) for k, x, y in zip(("rho", "u", "T", "q"), a, b)}
-        err["fp64_change_steps_400_500"] = {k: relerr(x, y) for k, x, y in zip(("rho", "u", "T", "q"), b400, b)}
 
         # ---- e2e through the C ABI with pinned host buffers
         hr, hu, hT = pinned(C), pinned(3 * C), pinned(C)
@@ -786,7 +790,7 @@ def main() -> int:
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "run_ok": ok,
             "fp64_value": fp64_value, "fp64_ms_per_step": ms64 / K64, "fp32_over_fp64": value / world / fp64_value,
-            "fp32_error_vs_fp64": {"steps": nerr, **err},
+            "fp32_error_vs_fp64": {"steps": nerr, **err} if err else None,
             "phases_ms": phases,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak if achieved else None,
@@ -800,11 +804,13 @@ def main() -> int:
         }
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(12.0, os.cpu_count() or 1)
-        if not args.no_batched:
+        # the other configurations, the batch and the served streams: one GPU only (with N > 1 the
+        # replicas would repeat them and hold every GPU for minutes)
+        if not args.no_batched and extras:
             line["host_pipeline"] = run_host_pipeline(tmp)
             line["other_configs"] = run_other_configs(tmp)
             line["batched"] = run_batched(tmp)
-        if not args.no_served:
+        if not args.no_served and extras:
             line["served"] = run_served(tmp, count=args.served_count, members=args.served_members)
             line["served_config5"] = run_served_config5(tmp, count=args.served5_count, members=args.served_members)
         if rank == 0:
