@@ -74,6 +74,7 @@ struct meso_oracle {
     V *u_res, *q_res;
     int step, run_state, converged, converge_state;
     double last_res[8]; /* the last check's residual list, in the reference's print order */
+    int round_fp32;     /* test hook: 1 = round the stored g - g0, h - h0 to FP32 after every step */
     int nres;
     double solution_time;
     Slice *slices;
@@ -858,6 +859,24 @@ static void after_step(meso_oracle *o) {
     }
 }
 
+/* Test hook (not part of the reference's algorithm): the stored distributions rounded as a
+ * storage of g - g0 and h - h0 in FP32 would round them, with g0 the Maxwellian at (rho0, u = 0,
+ * T0) and h0 = (K + 1) R T0 g0 (2-D), everything else in FP64.  Isolates the storage rounding of
+ * an FP32-storage step. */
+static void round_state_fp32(meso_oracle *o) {
+    const double RT0 = o->R * o->T0, over = 0.5 / RT0;
+    for (int p = 0; p < o->NV; ++p) {
+        const double x = o->xi[p].x, y = o->xi[p].y;
+        const double g0 = o->par.rho0 * over / PI * exp(-(x * x + y * y) * over);
+        const double h0 = (o->K + 1.0) * RT0 * g0;
+        for (int c = 0; c < o->C; ++c) {
+            double *gp = &G(o->g, p, c, o->C), *hp = &G(o->h, p, c, o->C);
+            *gp = g0 + (double)(float)(*gp - g0);
+            *hp = h0 + (double)(float)(*hp - h0);
+        }
+    }
+}
+
 typedef struct {
     meso_oracle *o;
     int tid, nsteps, *done;
@@ -871,6 +890,7 @@ static void *run_steps(void *arg) {
         if (o->solver == MESO_SOLVER_CDUGKS_SHAKHOV) {
             shakhov_step(o, j->tid);
             if (j->tid == 0) shakhov_finish(o);
+            if (j->tid == 0 && o->round_fp32) round_state_fp32(o);
         } else {
             bgk_step(o, j->tid);
             if (j->tid == 0) {
@@ -1170,6 +1190,12 @@ int mo_get_state(const meso_oracle *o, int32_t *step, int32_t *run_state, int32_
     if (run_state) *run_state = o->run_state;
     if (converged) *converged = o->converged;
     if (t) *t = o->solution_time;
+    return MESO_OK;
+}
+
+int mo_set_storage_rounding(meso_oracle *o, int32_t on) {
+    if (!o || o->solver != MESO_SOLVER_CDUGKS_SHAKHOV || o->dim != 2) return MESO_ERR_INVALID;
+    o->round_fp32 = on ? 1 : 0;
     return MESO_OK;
 }
 

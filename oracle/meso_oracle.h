@@ -46,6 +46,10 @@ int mo_get_state(const meso_oracle *o, int32_t *step, int32_t *run_state, int32_
 /* the last residual check's list (Res[Rho], Res[T], Res[u], ... in the reference's print order;
  * cdugks_shakhov.cpp:729-746, cdugks.cpp:343-355) and its length (0 before the first check) */
 int mo_get_residual(const meso_oracle *o, double *list, int32_t *n);
+/* test hook (2-D Shakhov only): after every step round the stored g - g0, h - h0 to FP32 (g0 the
+ * Maxwellian at rho0, u = 0, T0), everything else staying FP64 -- the storage rounding of an
+ * FP32-storage step in isolation; not part of the reference's algorithm */
+int mo_set_storage_rounding(meso_oracle *o, int32_t on);
 /* distribution of velocity p at cell c (d = 0: f or g, 1: h) */
 double mo_get_f(const meso_oracle *o, int32_t d, int32_t p, int32_t c);
 int mo_set_params(meso_oracle *o, const meso_params *params);

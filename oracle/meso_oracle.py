@@ -45,6 +45,8 @@ def lib() -> C.CDLL:
         L.mo_get_state.restype = C.c_int
         L.mo_get_f.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
         L.mo_get_f.restype = C.c_double
+        L.mo_set_storage_rounding.argtypes = [vp, C.c_int32]
+        L.mo_set_storage_rounding.restype = C.c_int
         L.mo_get_residual.argtypes = [vp, dp, C.POINTER(C.c_int32)]
         L.mo_get_residual.restype = C.c_int
         L.mo_set_params.argtypes = [vp, vp]
@@ -233,6 +235,12 @@ class Oracle:
         t = C.c_double()
         lib().mo_get_state(self._h, C.byref(s), C.byref(r), C.byref(c), C.byref(t))
         return dict(step=s.value, run_state=r.value, converged=c.value, solution_time=t.value)
+
+    def set_storage_rounding(self, on: bool) -> None:
+        """Test hook: round the stored deviations from the reference Maxwellian to FP32 after every
+        step (2-D Shakhov), the storage rounding of the FP32 form in isolation."""
+        if lib().mo_set_storage_rounding(self._h, 1 if on else 0):
+            raise RuntimeError("mo_set_storage_rounding: 2-D Shakhov only")
 
     def residual(self) -> np.ndarray:
         """The last residual check's list, in the reference's print order."""
