@@ -74,7 +74,8 @@ struct meso_oracle {
     V *u_res, *q_res;
     int step, run_state, converged, converge_state;
     double last_res[8]; /* the last check's residual list, in the reference's print order */
-    int round_fp32;     /* test hook: 1 = round the stored g - g0, h - h0 to FP32 after every step */
+    int round_fp32;     /* test hook: round the stored g - g0, h - h0 to FP32 after every step, 1 to
+                           nearest, 2 stochastically */
     int nres;
     double solution_time;
     Slice *slices;
@@ -863,16 +864,39 @@ static void after_step(meso_oracle *o) {
  * storage of g - g0 and h - h0 in FP32 would round them, with g0 the Maxwellian at (rho0, u = 0,
  * T0) and h0 = (K + 1) R T0 g0 (2-D), everything else in FP64.  Isolates the storage rounding of
  * an FP32-storage step. */
+/* 32-bit mix of (a, b, c) (a multiply-xorshift hash), uniform in [0, 1) as a double */
+static double hash_unit(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u ^ (c + 0x165667B1u) * 0xC2B2AE3Du;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return (double)h * (1.0 / 4294967296.0);
+}
+
+/* x rounded to FP32: to nearest (mode 1) or stochastically (mode 2: up with probability equal to
+   the distance from the float below, in units of the gap, drawn from hash_unit(key...)) */
+static double to_fp32(double x, int mode, uint32_t k0, uint32_t k1, uint32_t k2) {
+    const float f = (float)x;
+    if (mode != 2 || (double)f == x) return (double)f;
+    const float lo = (double)f < x ? f : nextafterf(f, -INFINITY);
+    const float hi = nextafterf(lo, INFINITY);
+    const double p = (x - (double)lo) / ((double)hi - (double)lo);
+    return hash_unit(k0, k1, k2) < p ? (double)hi : (double)lo;
+}
+
 static void round_state_fp32(meso_oracle *o) {
     const double RT0 = o->R * o->T0, over = 0.5 / RT0;
+    const int mode = o->round_fp32;
     for (int p = 0; p < o->NV; ++p) {
         const double x = o->xi[p].x, y = o->xi[p].y;
         const double g0 = o->par.rho0 * over / PI * exp(-(x * x + y * y) * over);
         const double h0 = (o->K + 1.0) * RT0 * g0;
         for (int c = 0; c < o->C; ++c) {
             double *gp = &G(o->g, p, c, o->C), *hp = &G(o->h, p, c, o->C);
-            *gp = g0 + (double)(float)(*gp - g0);
-            *hp = h0 + (double)(float)(*hp - h0);
+            *gp = g0 + to_fp32(*gp - g0, mode, (uint32_t)c, (uint32_t)(2 * p), (uint32_t)o->step);
+            *hp = h0 + to_fp32(*hp - h0, mode, (uint32_t)c, (uint32_t)(2 * p + 1), (uint32_t)o->step);
         }
     }
 }
@@ -1195,7 +1219,8 @@ int mo_get_state(const meso_oracle *o, int32_t *step, int32_t *run_state, int32_
 
 int mo_set_storage_rounding(meso_oracle *o, int32_t on) {
     if (!o || o->solver != MESO_SOLVER_CDUGKS_SHAKHOV || o->dim != 2) return MESO_ERR_INVALID;
-    o->round_fp32 = on ? 1 : 0;
+    if (on < 0 || on > 2) return MESO_ERR_INVALID;
+    o->round_fp32 = on;
     return MESO_OK;
 }
 

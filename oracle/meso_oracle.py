@@ -236,10 +236,12 @@ class Oracle:
         lib().mo_get_state(self._h, C.byref(s), C.byref(r), C.byref(c), C.byref(t))
         return dict(step=s.value, run_state=r.value, converged=c.value, solution_time=t.value)
 
-    def set_storage_rounding(self, on: bool) -> None:
+    def set_storage_rounding(self, on: bool, stochastic: bool = False) -> None:
         """Test hook: round the stored deviations from the reference Maxwellian to FP32 after every
-        step (2-D Shakhov), the storage rounding of the FP32 form in isolation."""
-        if lib().mo_set_storage_rounding(self._h, 1 if on else 0):
+        step (2-D Shakhov), the storage rounding of the FP32 form in isolation: to nearest, or
+        stochastically (up with probability equal to the distance from the float below in units of
+        the gap, the draw a hash of cell, velocity and step)."""
+        if lib().mo_set_storage_rounding(self._h, (2 if stochastic else 1) if on else 0):
             raise RuntimeError("mo_set_storage_rounding: 2-D Shakhov only")
 
     def residual(self) -> np.ndarray:
