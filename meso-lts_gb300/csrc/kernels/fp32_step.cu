@@ -550,17 +550,22 @@ __global__ void __launch_bounds__(kT, 1) k32_reconstruct(const F32Inst *__restri
         load_chunk<VPL>(S, NVp, ch0, 0, sm);
         for (int ch = ch0; ch < ch1; ++ch) {
             const int buf = (ch - ch0) & 1;
-            next_chunk<VPL>(S, NVp, ch, ch1, buf, sm);
-            gradients(sm, buf, grad_on);
-            __syncthreads();
-            float hx[VPL], hy[VPL];
+            // the chunk's velocities first: their loads overlap the wait, the gradients and the barriers
+            float2 xv[VPL];
             int p[VPL];
 #pragma unroll
             for (int v = 0; v < VPL; ++v) {
                 p[v] = ch * SEG + v * 32 + lane;
-                const float4 t = vt32[p[v]];
-                hx[v] = hdt * t.x;
-                hy[v] = hdt * t.y;
+                xv[v] = *reinterpret_cast<const float2 *>(&vt32[p[v]]);
+            }
+            next_chunk<VPL>(S, NVp, ch, ch1, buf, sm);
+            gradients(sm, buf, grad_on);
+            __syncthreads();
+            float hx[VPL], hy[VPL];
+#pragma unroll
+            for (int v = 0; v < VPL; ++v) {
+                hx[v] = hdt * xv[v].x;
+                hy[v] = hdt * xv[v].y;
             }
 #pragma unroll 2
             for (int fl = warp; fl < nOF; fl += kRW) {
@@ -663,10 +668,7 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
         load_upd_chunk<VPL>(S, NVp, ch0, 0, sm);
         for (int ch = ch0; ch < ch1; ++ch) {
             const int buf = (ch - ch0) & 1;
-            // chunk ch visible; every warp has finished chunk ch - 1, so its buffer takes chunk ch + 1
-            cp_async_wait<0>();
-            __syncthreads();
-            if (ch + 1 < ch1) load_upd_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
+            // the chunk's velocity table first: its loads overlap the wait and the barrier below
             float xx[VPL], xy[VPL], w[VPL], g0[VPL], x2[VPL];
             int p[VPL];
 #pragma unroll
@@ -675,10 +677,15 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
                 const float4 t = vt32[p[v]];
                 xx[v] = t.x;
                 xy[v] = t.y;
-                x2[v] = fmaf(xx[v], xx[v], xy[v] * xy[v]);
                 w[v] = t.z;
                 g0[v] = t.w;
             }
+            // chunk ch visible; every warp has finished chunk ch - 1, so its buffer takes chunk ch + 1
+            cp_async_wait<0>();
+            __syncthreads();
+            if (ch + 1 < ch1) load_upd_chunk<VPL>(S, NVp, ch + 1, buf ^ 1, sm);
+#pragma unroll
+            for (int v = 0; v < VPL; ++v) x2[v] = fmaf(xx[v], xx[v], xy[v] * xy[v]);
 #pragma unroll
             for (int r = 0; r < RC; ++r) {
                 const int cl = warp + kUW * r;
