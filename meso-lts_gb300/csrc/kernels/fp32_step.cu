@@ -785,7 +785,7 @@ __global__ void __launch_bounds__(256) k32_face_moments(const F32Inst *__restric
             for (int j = 0; j < NB; ++j) {
                 const int p = p0 + 32 * j + lane;
                 tv[j] = p < I.NVp ? vt32[p] : make_float4(0.f, 0.f, 0.f, 0.f);
-                gv[j] = p < I.NVp ? src[p] : make_float2(0.f, 0.f);
+                gv[j] = p < I.NVp ? __ldcs(&src[p]) : make_float2(0.f, 0.f);  // read once: evict first
             }
             float m[F32_NMOM];
 #pragma unroll
@@ -864,7 +864,7 @@ __global__ void __launch_bounds__(256) k32_face_moments_small(const F32Inst *__r
                 for (int j = 0; j < NB; ++j) {
                     const int p = p0 + L * j + sl;
                     tv[j] = p < I.NVp ? vt32[p] : make_float4(0.f, 0.f, 0.f, 0.f);
-                    gv[j] = p < I.NVp ? src[p] : make_float2(0.f, 0.f);
+                    gv[j] = p < I.NVp ? __ldcs(&src[p]) : make_float2(0.f, 0.f);  // read once: evict first
                 }
                 float m[F32_NMOM];
 #pragma unroll
