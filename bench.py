@@ -312,9 +312,11 @@ def run_other_configs(tmp: str) -> dict:
     c3 = mg.Case(p3)
     rho, u, T, mask = c3.initial_fields()
     res = {}
-    for prec in (mg.FP32, mg.FP64):  # the workload's 5000 steps; 200 of them timed
-        s = mg.Solver(case=c3, precision=prec, mask=mask)
+    for prec in (mg.FP32, mg.FP64, "refined"):  # the workload's 5000 steps; 200 of them timed
+        s = mg.Solver(case=c3, precision=mg.FP32 if prec == "refined" else prec, mask=mask)
         s.init_macros(rho, u, T, None, 0)
+        if prec == "refined":  # FP32 with an FP64 defect correction every 20 steps
+            s.refine(20)
         s.step(3)
         s.step(200)
         ms = s.last_step_ms() / 200
@@ -331,6 +333,13 @@ def run_other_configs(tmp: str) -> dict:
                                    "value": cx3 / (res[mg.FP32][0] * 1e-3), "unit": UNIT,
                                    "ms_per_step": res[mg.FP32][0], "fp64_ms_per_step": res[mg.FP64][0],
                                    "fp32_error_vs_fp64": e32, "fp64_change_steps_4900_5000": drift,
+                                   "refined_every_20": {
+                                       "ms_per_step": res["refined"][0],
+                                       "error_vs_fp64": {k: relerr(comps(res["refined"][1])[k], v)
+                                                         for k, v in comps(res[mg.FP64][1]).items()},
+                                       "note": "meso_fp32_refine(20): one FP64 step and one FP32 step from the "
+                                               "same state every 20 steps measure the FP32 step's error, which the "
+                                               "FP32 steps between add back"},
                                    "note": "state 23 MB fits in L2; CFL 0.5 (at 0.8 the reference blows up at step "
                                            "140, tests/golden/config3_cfl08_blowup.npz)"}
     return out

@@ -270,6 +270,20 @@ int meso_initial(meso_ctx *ctx);
  */
 int meso_step(meso_ctx *ctx, int32_t nsteps, int32_t *steps_done);
 
+/*
+ * Defect correction of the FP32 form (2-D Shakhov FP32 contexts; no counterpart in the reference,
+ * whose step is FP64).  With interval > 0, every interval-th step of meso_step runs the plain
+ * FP64 step (the reference's arithmetic) and the FP32 step from the same state, keeps their
+ * difference as a correction that every following FP32 step adds to its results (state, the
+ * conservative update, the heat flux; the state rounded stochastically), and continues from the
+ * FP64 step's result.  The FP32 form's fields then settle to the FP64 step's steady state instead
+ * of one displaced by the FP32 arithmetic's rounding.  Costs the FP64 step's buffers on the device
+ * (about 64 bytes per cell-velocity) and one FP64 + one FP32 step per interval; the corrections
+ * start from zero when switched on and are not part of meso_snapshot.  interval = 0 switches it
+ * off.  MESO_ERR_UNSUPPORTED for other contexts, MESO_ERR_INVALID for batch members.
+ */
+int meso_fp32_refine(meso_ctx *ctx, int32_t interval);
+
 /* Macroscopic cell fields rho_cell, vel_cell, T_cell, q_cell (any pointer may be NULL). */
 int meso_get_macros(meso_ctx *ctx, double *rho, double *u, double *T, double *q);
 

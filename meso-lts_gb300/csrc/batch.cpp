@@ -153,6 +153,8 @@ int meso_batch_create(meso_ctx *const *ctxs, int32_t n, meso_batch **out) {
             return fail(MESO_ERR_UNSUPPORTED, "batches step FP32 contexts only");
         if (!c->initialized) return fail(MESO_ERR_INVALID, "batch member " + std::to_string(i) + " is not initialised");
         if (c->batch) return fail(MESO_ERR_INVALID, "context is already in a batch");
+        if (c->f32.corrS)
+            return fail(MESO_ERR_UNSUPPORTED, "a context with defect correction (meso_fp32_refine) steps alone");
         if (c->device != m[0]->device) return fail(MESO_ERR_INVALID, "batch members must share a device");
         for (int j = 0; j < i; ++j)
             if (m[j] == c) return fail(MESO_ERR_INVALID, "context listed twice");

@@ -962,6 +962,95 @@ int meso_initial(meso_ctx *c) {
     }
 }
 
+// One step of an FP32 context with defect correction: the FP64 step from the current state (its
+// step counter and flags put back afterwards), the corrected FP32 step from the same state, then
+// the corrections take the difference and the state continues from the FP64 result.
+static int refine_step(meso_ctx *c) {
+    const auto &I = c->f32;
+    auto &s = c->ps64;
+    s.kp = c->ps.kp;  // the current step settings
+    if (meso::fp32_to_plain(I, c->fs.d_inst, s.f0, s.f1, s.rho, c->num_sms, c->stream))
+        return fail(MESO_ERR_CUDA, std::string("refine: ") + cudaGetErrorString(cudaGetLastError()));
+    CUDA_TRY(cudaMemcpyAsync(c->d_status_save, c->d_status, sizeof(meso::DStatus), cudaMemcpyDeviceToDevice, c->stream));
+    if (meso::plain_step(s, c->stream, &c->last_launches))
+        return fail(MESO_ERR_CUDA, std::string("refine: FP64 step: ") + cudaGetErrorString(cudaGetLastError()));
+    CUDA_TRY(cudaMemcpyAsync(c->d_status, c->d_status_save, sizeof(meso::DStatus), cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(cudaMemsetAsync(c->refine_pass, 0xff, sizeof(int), c->stream));
+    int rc = launch_step(c);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemsetAsync(c->refine_pass, 0, sizeof(int), c->stream));
+    if (meso::fp32_refine(I, c->fs.d_inst, s.f0, s.f1, s.rho, c->num_sms, c->stream))
+        return fail(MESO_ERR_CUDA, std::string("refine: ") + cudaGetErrorString(cudaGetLastError()));
+    return MESO_OK;
+}
+
+int meso_fp32_refine(meso_ctx *c, int32_t interval) {
+    CTX_CHECK(c);
+    if (interval < 0) return fail(MESO_ERR_INVALID, "interval must be >= 0");
+    if (c->params.precision != MESO_FP32 || c->params.solver != MESO_SOLVER_CDUGKS_SHAKHOV || c->dim != 2)
+        return fail(MESO_ERR_UNSUPPORTED, "defect correction applies to 2-D Shakhov FP32 contexts");
+    if (c->batch) return fail(MESO_ERR_INVALID, "a batch member steps with its batch: leave the batch first");
+    auto &I = c->f32;
+    const size_t C = (size_t)c->C;
+    if (interval > 0 && !c->corrS_mem) {  // first use: the corrections and the FP64 step's buffers
+        auto &A = c->arena;
+        auto &s = c->ps64;
+        s.solver = c->params.solver;
+        s.num_sms = c->num_sms;
+        s.mesh = c->dm;
+        s.status = c->d_status;
+        const size_t cv = C * (size_t)c->NV, fv = (size_t)c->F * (size_t)c->NV;
+        const size_t bv = (size_t)std::max(c->nb, 1) * (size_t)c->NV;
+        try {
+            c->corrS_mem = A.alloc<float2>(C * (size_t)I.NVp);
+            c->corrW_mem = A.alloc<double>(4 * C);
+            c->corrq_mem = A.alloc<double>(2 * C);
+            c->corrR_mem = A.alloc<float2>(C * (size_t)I.NVp);
+            c->refine_pass = A.alloc<int>(1);
+            CUDA_TRY(cudaMemsetAsync(c->refine_pass, 0, sizeof(int), c->stream));
+            s.f0 = A.alloc<double>(cv);
+            s.f1 = A.alloc<double>(cv);
+            s.face0 = A.alloc<double>(fv);
+            s.face1 = A.alloc<double>(fv);
+            s.grad0 = A.alloc<double>(cv * 2);
+            s.grad1 = A.alloc<double>(cv * 2);
+            s.flux0 = A.alloc<double>(cv);
+            s.flux1 = A.alloc<double>(cv);
+            s.snap0 = A.alloc<double>(bv);
+            s.snap1 = A.alloc<double>(bv);
+            s.rho = A.alloc<double>(8 * C);
+            s.u = s.rho + C;
+            s.T = s.rho + 4 * C;
+            s.q = s.rho + 5 * C;
+            s.fm0 = A.alloc<double>(C);
+            s.fm1 = A.alloc<double>(3 * C);
+            s.fm2 = A.alloc<double>(C);
+            s.repair_list = A.alloc<int>(C);
+            c->d_status_save = A.alloc<meso::DStatus>(1);
+        } catch (const std::bad_alloc &) {
+            cudaGetLastError();
+            c->corrS_mem = nullptr;
+            return fail(MESO_ERR_OOM, "device allocation for the defect correction failed");
+        }
+    }
+    if (interval > 0 && !I.corrS) {  // switched on: the corrections start from zero
+        CUDA_TRY(cudaMemsetAsync(c->corrS_mem, 0, sizeof(float2) * C * (size_t)I.NVp, c->stream));
+        CUDA_TRY(cudaMemsetAsync(c->corrW_mem, 0, sizeof(double) * 4 * C, c->stream));
+        CUDA_TRY(cudaMemsetAsync(c->corrq_mem, 0, sizeof(double) * 2 * C, c->stream));
+    }
+    I.corrS = interval > 0 ? c->corrS_mem : nullptr;
+    I.corrW = interval > 0 ? c->corrW_mem : nullptr;
+    I.corrq = interval > 0 ? c->corrq_mem : nullptr;
+    I.corrR = interval > 0 ? c->corrR_mem : nullptr;
+    I.refine_pass = interval > 0 ? c->refine_pass : nullptr;
+    c->refine_interval = interval;
+    c->fs.corr = interval > 0 ? 1 : 0;
+    CUDA_TRY(cudaMemcpyAsync(c->fs.d_inst, &I, sizeof(I), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->f32_version++;
+    return MESO_OK;
+}
+
 int meso_step(meso_ctx *c, int32_t nsteps, int32_t *steps_done) {
     CTX_CHECK(c);
     if (steps_done) *steps_done = 0;
@@ -977,7 +1066,9 @@ int meso_step(meso_ctx *c, int32_t nsteps, int32_t *steps_done) {
     bool stopped = false;
     for (int i = 0; i < nsteps && c->run_state; ++i) {
         maybe_reload(c);
-        int rc = launch_step(c);
+        const int ki = c->refine_interval;
+        int rc = ki > 0 && c->params.precision == MESO_FP32 && (start + issued) % ki == 0 ? refine_step(c)
+                                                                                       : launch_step(c);
         if (rc) return rc;
         dts.push_back(c->params.dt);
         ++issued;

@@ -116,4 +116,13 @@ struct meso_ctx {
     meso::KParams plain_graph_kp{};
     int64_t plain_graph_launches = 0;
     meso_batch *batch = nullptr;  // the batch this context is a member of, if any
+    // FP32 defect correction (meso_fp32_refine): every refine_interval steps one FP64 step from the
+    // same state (ps, with its own buffers) measures the FP32 step's error
+    int refine_interval = 0;
+    meso::PlainState ps64{};      // the FP64 step's own buffers (ps aliases the FP32 instance's macros)
+    meso::DStatus *d_status_save = nullptr;
+    float2 *corrS_mem = nullptr;  // the corrections' device arrays, kept while the correction is off
+    double *corrW_mem = nullptr, *corrq_mem = nullptr;
+    float2 *corrR_mem = nullptr;
+    int *refine_pass = nullptr;
 };

@@ -110,6 +110,28 @@ __device__ __forceinline__ float expm1_dev(float x) {
     return fabsf(x) < 0.5f ? series : direct;
 }
 
+// 32 random bits from three keys (a multiply-xorshift mix): the draws of stochastic rounding.
+__device__ __forceinline__ unsigned mix3(unsigned a, unsigned b, unsigned c) {
+    unsigned h = a ^ b ^ c;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return h;
+}
+// x + r stochastically rounded to FP32 (x the value rounded to nearest, r its residual, |r| at
+// most half a unit in the last place): x + r plus a dither uniform over one unit in the last place
+// of x, rounded to nearest, rounds up with probability equal to the distance from the float below
+// (16 random bits).  Zero, subnormal and non-finite x come back unchanged.
+__device__ __forceinline__ float sr_round(float x, float r, unsigned bits16) {
+    const unsigned e = __float_as_uint(x) & 0x7f800000u;
+    if (e == 0u || e == 0x7f800000u) return x;
+    const float ulp = __uint_as_float(e) * 1.1920928955078125e-7f;  // 2^(exponent - 23)
+    const float u = __uint_as_float(0x3f800000u | (bits16 << 7)) - 1.5f;  // [-1/2, 1/2)
+    return x + fmaf(u, ulp, r);
+}
+
 // Deviation of the Shakhov g, h (2-D, cdugks_shakhov.cpp:185-211) at one velocity
 // from the reference pair (g0, hm0 g0):
 //   g_M = g0 + dg_M,  dg_M = g0 expm1(E)
@@ -210,6 +232,7 @@ __device__ __forceinline__ void g0_fluxes(const F32Inst &I, double nx, double ny
 // instruction; the (g, h) pairs of the step map onto them.
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 
@@ -607,7 +630,10 @@ __device__ __forceinline__ void load_upd_chunk(const float2 *S, int NVp, int ch,
     cp_async_commit();
 }
 
-template <int VPL>
+// CORR: the instance carries defect corrections; each stored value is the FP32 result plus its
+// correction, rounded stochastically (round to nearest would return the same value every step at
+// a steady state and the corrected iteration would stall short of it).
+template <int VPL, bool CORR>
 __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__ insts, const int4 *__restrict__ items,
                                                    const int *__restrict__ item_off) {
     constexpr int SEG = UpdSmem<VPL>::SEG;
@@ -619,6 +645,7 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
         const F32Inst &I = insts[item.x];
         if (step_stopped(I.status)) continue;
         const int cur = I.status->step & 1;  // S[step parity] holds the current state
+        const bool measure = CORR && *I.refine_pass != 0;
         const int tile = item.y, grp = item.z;
         const int cs = I.tile_cstart[tile], nc = I.tile_ncell[tile];
         const int ch0 = item.w & 0xffff, ch1 = item.w >> 16;
@@ -730,7 +757,28 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
                     e = fma2(f2(k.hdt_taun), sub2(sn, gn), e);
                     e = fma2(f2(-k.dt_v), fl[v], e);
                     const float2 gh = mul2(f2(k.C), e);
-                    Sn[(size_t)(cs + cl) * NVp + p[v]] = fma2(f2(k.Cs), sub2(s1, gh), gh);
+                    const size_t at = (size_t)(cs + cl) * NVp + p[v];
+                    if (CORR) {
+                        // C (...) + Cs (g_S - C (...)) + correction: the fused result, the residual of
+                        // its rounding, the correction added with its error (|correction| is small)
+                        const float2 d1 = sub2(s1, gh);
+                        const float2 xs = fma2(f2(k.Cs), d1, gh);
+                        const float2 rs = fma2(f2(k.Cs), d1, sub2(gh, xs));
+                        const float2 cS = I.corrS[at];
+                        const float2 y = add2(xs, cS);
+                        const float2 r = add2(rs, sub2(cS, sub2(y, xs)));
+                        if (measure) {
+                            Sn[at] = y;
+                            I.corrR[at] = r;
+                        } else {
+                            const unsigned hb = mix3((unsigned)(cs + cl) * 0x9E3779B1u,
+                                                     (unsigned)p[v] * 0x85EBCA77u,
+                                                     (unsigned)I.status->step * 0xC2B2AE3Du);
+                            Sn[at] = make_float2(sr_round(y.x, r.x, hb & 0xffffu), sr_round(y.y, r.y, hb >> 16));
+                        }
+                    } else {
+                        Sn[at] = fma2(f2(k.Cs), sub2(s1, gh), gh);
+                    }
                     // heat-flux partial (:692)
                     const float hw = 0.5f * w[v] * fmaf(cc, gh.x, gh.y);
                     qv[0] = fmaf(hw, cx, qv[0]);
@@ -1463,9 +1511,16 @@ __global__ void k32_cell_macros(const F32Inst *__restrict__ insts, const int *__
         const double rhoE_n = rho_n * (0.5 * (unx * unx + uny * uny) + I.Cv * T_n);
         const double irho_n = 1.0 / rho_n, iT_n = 1.0 / T_n;
         const double tau_n = tau_r(I, irho_n, T_n, iT_n);
-        const double rho = rho_n - dt_v * m0;
-        const double rux = rho_n * unx - dt_v * m1x, ruy = rho_n * uny - dt_v * m1y;
-        const double rhoE = rhoE_n - dt_v * 0.5 * m2;
+        double rho = rho_n - dt_v * m0;
+        double rux = rho_n * unx - dt_v * m1x, ruy = rho_n * uny - dt_v * m1y;
+        double rhoE = rhoE_n - dt_v * 0.5 * m2;
+        if (I.corrW) {  // defect correction of the conserved update
+            const double *cw = I.corrW + 4 * (size_t)c;
+            rho += cw[0];
+            rux += cw[1];
+            ruy += cw[2];
+            rhoE += cw[3];
+        }
         const double irho = 1.0 / rho;
         const double ux = rux * irho, uy = ruy * irho;
         const double T = (rhoE * irho - 0.5 * (ux * ux + uy * uy)) * I.iCv, iT = 1.0 / T;
@@ -1524,6 +1579,10 @@ __global__ void k32_heat_flux(const F32Inst *__restrict__ insts, const int *__re
             g0_raw_moments(I, I.u[3 * c], I.u[3 * c + 1], M0);
             qx += 0.5 * (M0[6] + M0[9]);
             qy += 0.5 * (M0[7] + M0[10]);
+        }
+        if (I.corrq) {  // defect correction
+            qx += I.corrq[2 * (size_t)c];
+            qy += I.corrq[2 * (size_t)c + 1];
         }
         I.q[3 * c] = qx;
         I.q[3 * c + 1] = qy;
@@ -1733,6 +1792,73 @@ __global__ void k32_init(const F32Inst *__restrict__ insts, const int *__restric
     }
 }
 
+// ---- defect correction (fp32_to_plain, fp32_refine) ------------------------------
+// The FP32 state in the FP64 step's layout: f0 = g0 + (g - g0), f1 = hm0 g0 + (h - h0), [C][NV].
+__global__ void k32_to_plain(const F32Inst *__restrict__ inst, double *__restrict__ f0, double *__restrict__ f1) {
+    const F32Inst &I = *inst;
+    const float2 *__restrict__ S = I.S[I.status->step & 1];
+    for (int c = blockIdx.x; c < I.C; c += gridDim.x)
+        for (int p = threadIdx.x; p < I.NV; p += blockDim.x) {
+            const float2 x = S[(size_t)c * I.NVp + p];
+            const double g0 = I.g0_64[p];
+            f0[(size_t)c * I.NV + p] = g0 + (double)x.x;
+            f1[(size_t)c * I.NV + p] = I.hm0 * g0 + (double)x.y;
+        }
+}
+
+// After one (corrected) FP32 step and one FP64 step from the same state: the state's correction
+// takes the FP64 result minus the FP32 one, and the FP32 result is replaced by the FP64 one.
+__global__ void k32_refine_state(const F32Inst *__restrict__ inst, const double *__restrict__ f0,
+                                 const double *__restrict__ f1) {
+    const F32Inst &I = *inst;
+    if (step_stopped(I.status)) return;
+    float2 *__restrict__ S = I.S[I.status->step & 1];
+    for (int c = blockIdx.x; c < I.C; c += gridDim.x)
+        for (int p = threadIdx.x; p < I.NV; p += blockDim.x) {
+            const size_t at = (size_t)c * I.NVp + p, ip = (size_t)c * I.NV + p;
+            const double g0 = I.g0_64[p];
+            const double gd = f0[ip] - g0, hd = f1[ip] - I.hm0 * g0;
+            // the FP32 step's value before rounding: the stored value and its residual
+            const float2 x = S[at], r = I.corrR[at], cs = I.corrS[at];
+            const double xg = (double)x.x + (double)r.x, xh = (double)x.y + (double)r.y;
+            I.corrS[at] = make_float2((float)((double)cs.x + (gd - xg)), (float)((double)cs.y + (hd - xh)));
+            // the FP64 result, rounded stochastically like every corrected step
+            const float ng = (float)gd, nh = (float)hd;
+            const unsigned hb = mix3((unsigned)c * 0x9E3779B1u, (unsigned)p * 0x85EBCA77u,
+                                     (unsigned)I.status->step * 0xC2B2AE3Du ^ 0x5bd1e995u);
+            S[at] = make_float2(sr_round(ng, (float)(gd - (double)ng), hb & 0xffffu),
+                                sr_round(nh, (float)(hd - (double)nh), hb >> 16));
+        }
+}
+
+// The same for the macros: the corrections of the conserved update and of the heat flux, then the
+// FP64 step's rho, u, T, q (mac: the 8C block rho [C], u [3C], T [C], q [3C]).
+__global__ void k32_refine_cells(const F32Inst *__restrict__ inst, const double *__restrict__ mac) {
+    const F32Inst &I = *inst;
+    if (step_stopped(I.status)) return;
+    const int C = I.C;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+        const double r64 = mac[c], ux64 = mac[C + 3 * c], uy64 = mac[C + 3 * c + 1], T64 = mac[4 * C + c];
+        const double qx64 = mac[5 * C + 3 * c], qy64 = mac[5 * C + 3 * c + 1];
+        const double r32 = I.rho[c], ux32 = I.u[3 * c], uy32 = I.u[3 * c + 1], T32 = I.T[c];
+        double *cw = I.corrW + 4 * (size_t)c;
+        cw[0] += r64 - r32;
+        cw[1] += r64 * ux64 - r32 * ux32;
+        cw[2] += r64 * uy64 - r32 * uy32;
+        cw[3] += r64 * (0.5 * (ux64 * ux64 + uy64 * uy64) + I.Cv * T64) -
+                 r32 * (0.5 * (ux32 * ux32 + uy32 * uy32) + I.Cv * T32);
+        I.corrq[2 * (size_t)c] += qx64 - I.q[3 * c];
+        I.corrq[2 * (size_t)c + 1] += qy64 - I.q[3 * c + 1];
+        I.rho[c] = r64;
+        I.u[3 * c] = ux64;
+        I.u[3 * c + 1] = uy64;
+        I.T[c] = T64;
+        I.q[3 * c] = qx64;
+        I.q[3 * c + 1] = qy64;
+        I.u32[c] = make_float2((float)ux64, (float)uy64);
+    }
+}
+
 int grid_of(int total, int per_block, int cap) {
     int b = (total + per_block - 1) / per_block;
     return b < 1 ? 1 : (b < cap ? b : cap);
@@ -1744,9 +1870,15 @@ int fp32_configure(int device) {
     (void)device;
     const int a1 = (int)tile_smem<1>(), a2 = (int)tile_smem<2>();
     if (cudaFuncSetAttribute(k32_reconstruct<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, a1) != cudaSuccess ||
-        cudaFuncSetAttribute(k32_update<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<1>()) != cudaSuccess ||
+        cudaFuncSetAttribute(k32_update<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<1>()) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k32_update<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<1>()) !=
+            cudaSuccess ||
         cudaFuncSetAttribute(k32_reconstruct<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, a2) != cudaSuccess ||
-        cudaFuncSetAttribute(k32_update<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<2>()) != cudaSuccess)
+        cudaFuncSetAttribute(k32_update<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<2>()) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k32_update<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<2>()) !=
+            cudaSuccess)
         return -1;
     return 0;
 }
@@ -1764,12 +1896,16 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     int n = 0;
     auto tiles = [&](bool update) {
         if (grid2 > 0) {
-            if (update) k32_update<2><<<grid2, kUT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
+            if (update && s.corr)
+                k32_update<2, true><<<grid2, kUT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
+            else if (update)
+                k32_update<2, false><<<grid2, kUT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
             else k32_reconstruct<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
             ++n;
         }
         if (grid1 > 0) {
-            if (update) k32_update<1><<<grid1, kUT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
+            if (update && s.corr) k32_update<1, true><<<grid1, kUT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
+            else if (update) k32_update<1, false><<<grid1, kUT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
             else k32_reconstruct<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
             ++n;
         }
@@ -1852,6 +1988,21 @@ int fp32_prepare(const Fp32State &s, cudaStream_t stream) {
     if (s.total_bnd > 0)
         k32_bnd_setup<<<grid_of(s.total_bnd, 1, s.num_sms * 32), 256, 0, stream>>>(s.d_inst, s.d_bnd_items, s.ninst,
                                                                                  s.total_bnd);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int fp32_to_plain(const F32Inst &I, const F32Inst *d_inst, double *f0, double *f1, double *mac, int sms,
+                  cudaStream_t stream) {
+    k32_to_plain<<<grid_of(I.C, 1, sms * 8), 256, 0, stream>>>(d_inst, f0, f1);
+    if (cudaMemcpyAsync(mac, I.rho, sizeof(double) * 8 * (size_t)I.C, cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+        return -1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int fp32_refine(const F32Inst &I, const F32Inst *d_inst, const double *f0, const double *f1, const double *mac,
+                int sms, cudaStream_t stream) {
+    k32_refine_state<<<grid_of(I.C, 1, sms * 8), 256, 0, stream>>>(d_inst, f0, f1);
+    k32_refine_cells<<<grid_of(I.C, 256, sms * 4), 256, 0, stream>>>(d_inst, mac);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -128,6 +128,15 @@ struct F32Inst {
     DStatus *status;
     F32Resid *resid;           // residual state (device)
     double *rho_old, *u_old, *T_old, *q_old;  // macros at the last residual check
+    // defect correction (null when off): added to each step's FP32 results so that the step
+    // reproduces the FP64 step at the state it was last measured on (fp32_refine)
+    float2 *corrS;         // [C][NVp] stored state (g - g0, h - h0)
+    double *corrW;         // [C][4] rho, rho ux, rho uy, rho E after the conservative update
+    double *corrq;         // [C][2] heat flux
+    float2 *corrR;         // [C][NVp] on a measuring step: the rounding residual of each stored value
+    int *refine_pass;      // device flag: non-zero on a measuring step (the stored value rounded to
+                           // nearest and its residual kept, so the correction is measured without
+                           // the stochastic rounding's draw)
 };
 
 // Boundary faces of small velocity sets per boundary-kernel block (a warp each).
@@ -151,6 +160,7 @@ struct Fp32State {
     int has_small = 0, has_large = 0;  // instances with NVp <= / > F32_SMALL_NVP
     int total_faces = 0, total_cells = 0, total_bnd = 0;
     int num_sms = 0;
+    int corr = 0;                // the single instance carries defect corrections (corrS non-null)
 };
 
 int fp32_configure(int device);
@@ -171,5 +181,15 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
 // Once per instance set-up, after the instances are on the device.
 int fp32_prepare(const Fp32State &s, cudaStream_t stream);
 int fp32_init(const Fp32State &s, int mode, cudaStream_t stream);
+
+// Defect correction of a single 2-D Shakhov instance (I: its host copy; d_inst: the device copy).
+// fp32_to_plain writes the current state and macros in the FP64 step's layout (f0 = g, f1 = h
+// [C][NV], the 8C macro block rho); fp32_refine, called after one FP32 step from that state and
+// one FP64 step from its copy, adds the FP64 step's results minus the FP32 step's to the
+// corrections and replaces the FP32 step's results with the FP64 ones.
+int fp32_to_plain(const F32Inst &I, const F32Inst *d_inst, double *f0, double *f1, double *mac, int sms,
+                  cudaStream_t stream);
+int fp32_refine(const F32Inst &I, const F32Inst *d_inst, const double *f0, const double *f1, const double *mac,
+                int sms, cudaStream_t stream);
 
 }  // namespace meso

@@ -93,6 +93,7 @@ _SIGS = {
     "meso_init_macros": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.c_int32]),
     "meso_initial": (C.c_int, [C.c_void_p]),
     "meso_step": (C.c_int, [C.c_void_p, C.c_int32, _ip]),
+    "meso_fp32_refine": (C.c_int, [C.c_void_p, C.c_int32]),
     "meso_get_macros": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
     "meso_get_flux_moments": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
     "meso_get_status": (C.c_int, [C.c_void_p, C.POINTER(Status)]),
@@ -284,6 +285,10 @@ class Solver:
         if rc != OK:
             raise MesoError(rc, lib().meso_last_error().decode())
         return done.value
+
+    def refine(self, interval: int):
+        """FP32 defect correction every `interval` steps (0: off); meso_fp32_refine."""
+        _check(lib().meso_fp32_refine(self._h, interval))
 
     def macros(self, ncell: int):
         rho, u, T, q = np.zeros(ncell), np.zeros(3 * ncell), np.zeros(ncell), np.zeros(3 * ncell)
