@@ -161,6 +161,10 @@ public:
         if (!run_state_ || (p.residual_interval > 0 && step % p.residual_interval == 0)) sync();
     }
 
+    // FP32 contexts (2-D Shakhov): an FP64 defect correction every `interval` steps, 0 = off
+    // (meso_fp32_refine).
+    void refine(int interval) { check(meso_fp32_refine(ctx_, interval)); }
+
     void output() { check(meso_output(ctx_)); }
     bool get_run_state() const { return run_state_; }
     int max_step() const { return max_step_; }

@@ -55,3 +55,22 @@ def test_dropin_loop_matches_golden(gpu, tmp_path, name):
     assert np.array_equal(np.loadtxt(tmp_path / "f_rho.dat"), rho)
     assert np.array_equal(np.loadtxt(tmp_path / "f_u.dat"), u[:, 0])
     assert np.array_equal(np.loadtxt(tmp_path / "f_vel.dat").reshape(n, 3), u)
+
+
+@pytest.mark.gpu
+def test_dropin_fp32_with_refinement(gpu, tmp_path):
+    """--refine K through the drop-in class (MESO::GPU::Solver::refine): the FP32 form of a golden
+    Shakhov case with an FP64 defect correction every 5 steps, within the FP32 transient bars of
+    the reference's outputs."""
+    name = "shakhov_q8_hgh8"
+    d = tmp_path / name
+    shutil.copytree(os.path.join(GOLDEN, "cases", name), d)
+    out = tmp_path / "macros.bin"
+    r = _run(["case.txt", "fp32", "--refine", "5", "--dump", str(out)], str(d))
+    assert r.returncode == 0, r.stderr
+    raw = np.fromfile(out, dtype=np.float64)
+    n, step = int(raw[0]), int(raw[1])
+    rho, u, T = raw[3:3 + n], raw[3 + n:3 + 4 * n].reshape(n, 3), raw[3 + 4 * n:3 + 5 * n]
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    assert step == int(g["step"])
+    assert relerr(rho, g["rho"]) <= 2e-6 and relerr(u, g["u"]) <= 2e-5 and relerr(T, g["T"]) <= 2e-6
