@@ -975,10 +975,10 @@ static int refine_step(meso_ctx *c) {
     if (meso::plain_step(s, c->stream, &c->last_launches))
         return fail(MESO_ERR_CUDA, std::string("refine: FP64 step: ") + cudaGetErrorString(cudaGetLastError()));
     CUDA_TRY(cudaMemcpyAsync(c->d_status, c->d_status_save, sizeof(meso::DStatus), cudaMemcpyDeviceToDevice, c->stream));
-    CUDA_TRY(cudaMemsetAsync(c->refine_pass, 0xff, sizeof(int), c->stream));
-    int rc = launch_step(c);
-    if (rc) return rc;
-    CUDA_TRY(cudaMemsetAsync(c->refine_pass, 0, sizeof(int), c->stream));
+    c->fs.corr = 2;  // the measuring step, launched directly (the captured step is the corrected one)
+    const int rc = meso::fp32_step(c->fs, c->stream, &c->last_launches);
+    c->fs.corr = 1;
+    if (rc) return fail(MESO_ERR_CUDA, std::string("refine: FP32 step: ") + cudaGetErrorString(cudaGetLastError()));
     if (meso::fp32_refine(I, c->fs.d_inst, s.f0, s.f1, s.rho, c->num_sms, c->stream))
         return fail(MESO_ERR_CUDA, std::string("refine: ") + cudaGetErrorString(cudaGetLastError()));
     return MESO_OK;
@@ -1006,8 +1006,6 @@ int meso_fp32_refine(meso_ctx *c, int32_t interval) {
             c->corrW_mem = A.alloc<double>(4 * C);
             c->corrq_mem = A.alloc<double>(2 * C);
             c->corrR_mem = A.alloc<float2>(C * (size_t)I.NVp);
-            c->refine_pass = A.alloc<int>(1);
-            CUDA_TRY(cudaMemsetAsync(c->refine_pass, 0, sizeof(int), c->stream));
             s.f0 = A.alloc<double>(cv);
             s.f1 = A.alloc<double>(cv);
             s.face0 = A.alloc<double>(fv);
@@ -1042,7 +1040,6 @@ int meso_fp32_refine(meso_ctx *c, int32_t interval) {
     I.corrW = interval > 0 ? c->corrW_mem : nullptr;
     I.corrq = interval > 0 ? c->corrq_mem : nullptr;
     I.corrR = interval > 0 ? c->corrR_mem : nullptr;
-    I.refine_pass = interval > 0 ? c->refine_pass : nullptr;
     c->refine_interval = interval;
     c->fs.corr = interval > 0 ? 1 : 0;
     CUDA_TRY(cudaMemcpyAsync(c->fs.d_inst, &I, sizeof(I), cudaMemcpyHostToDevice, c->stream));

@@ -124,5 +124,4 @@ struct meso_ctx {
     float2 *corrS_mem = nullptr;  // the corrections' device arrays, kept while the correction is off
     double *corrW_mem = nullptr, *corrq_mem = nullptr;
     float2 *corrR_mem = nullptr;
-    int *refine_pass = nullptr;
 };

@@ -630,10 +630,12 @@ __device__ __forceinline__ void load_upd_chunk(const float2 *S, int NVp, int ch,
     cp_async_commit();
 }
 
-// CORR: the instance carries defect corrections; each stored value is the FP32 result plus its
-// correction, rounded stochastically (round to nearest would return the same value every step at
-// a steady state and the corrected iteration would stall short of it).
-template <int VPL, bool CORR>
+// MODE 0: plain.  MODE 1: the instance carries defect corrections; each stored value is the FP32
+// result plus its correction, rounded stochastically (round to nearest would return the same value
+// every step at a steady state and the corrected iteration would stall short of it).  MODE 2: a
+// measuring step of the correction: the value rounded to nearest, its rounding residual kept in
+// corrR, so that the correction is measured against the unrounded result.
+template <int VPL, int MODE>
 __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__ insts, const int4 *__restrict__ items,
                                                    const int *__restrict__ item_off) {
     constexpr int SEG = UpdSmem<VPL>::SEG;
@@ -645,7 +647,6 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
         const F32Inst &I = insts[item.x];
         if (step_stopped(I.status)) continue;
         const int cur = I.status->step & 1;  // S[step parity] holds the current state
-        const bool measure = CORR && *I.refine_pass != 0;
         const int tile = item.y, grp = item.z;
         const int cs = I.tile_cstart[tile], nc = I.tile_ncell[tile];
         const int ch0 = item.w & 0xffff, ch1 = item.w >> 16;
@@ -758,7 +759,7 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
                     e = fma2(f2(-k.dt_v), fl[v], e);
                     const float2 gh = mul2(f2(k.C), e);
                     const size_t at = (size_t)(cs + cl) * NVp + p[v];
-                    if (CORR) {
+                    if (MODE != 0) {
                         // C (...) + Cs (g_S - C (...)) + correction: the fused result, the residual of
                         // its rounding, the correction added with its error (|correction| is small)
                         const float2 d1 = sub2(s1, gh);
@@ -767,7 +768,7 @@ __global__ void __launch_bounds__(kUT, 1) k32_update(const F32Inst *__restrict__
                         const float2 cS = I.corrS[at];
                         const float2 y = add2(xs, cS);
                         const float2 r = add2(rs, sub2(cS, sub2(y, xs)));
-                        if (measure) {
+                        if (MODE == 2) {
                             Sn[at] = y;
                             I.corrR[at] = r;
                         } else {
@@ -1870,16 +1871,14 @@ int fp32_configure(int device) {
     (void)device;
     const int a1 = (int)tile_smem<1>(), a2 = (int)tile_smem<2>();
     if (cudaFuncSetAttribute(k32_reconstruct<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, a1) != cudaSuccess ||
-        cudaFuncSetAttribute(k32_update<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<1>()) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(k32_update<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<1>()) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(k32_reconstruct<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, a2) != cudaSuccess ||
-        cudaFuncSetAttribute(k32_update<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<2>()) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(k32_update<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem<2>()) !=
-            cudaSuccess)
+        cudaFuncSetAttribute(k32_reconstruct<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, a2) != cudaSuccess)
         return -1;
+    const int u1 = (int)upd_smem<1>(), u2 = (int)upd_smem<2>();
+    const void *fn[6] = {(const void *)k32_update<1, 0>, (const void *)k32_update<1, 1>, (const void *)k32_update<1, 2>,
+                         (const void *)k32_update<2, 0>, (const void *)k32_update<2, 1>, (const void *)k32_update<2, 2>};
+    for (int k = 0; k < 6; ++k)
+        if (cudaFuncSetAttribute(fn[k], cudaFuncAttributeMaxDynamicSharedMemorySize, k < 3 ? u1 : u2) != cudaSuccess)
+            return -1;
     return 0;
 }
 
@@ -1896,16 +1895,19 @@ int fp32_step(Fp32State &s, cudaStream_t stream, int64_t *launches, cudaEvent_t 
     int n = 0;
     auto tiles = [&](bool update) {
         if (grid2 > 0) {
-            if (update && s.corr)
-                k32_update<2, true><<<grid2, kUT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
+            if (update && s.corr == 2)
+                k32_update<2, 2><<<grid2, kUT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
+            else if (update && s.corr)
+                k32_update<2, 1><<<grid2, kUT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
             else if (update)
-                k32_update<2, false><<<grid2, kUT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
+                k32_update<2, 0><<<grid2, kUT, upd_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
             else k32_reconstruct<2><<<grid2, kT, tile_smem<2>(), stream>>>(s.d_inst, s.d_items, s.d_item_off);
             ++n;
         }
         if (grid1 > 0) {
-            if (update && s.corr) k32_update<1, true><<<grid1, kUT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
-            else if (update) k32_update<1, false><<<grid1, kUT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
+            if (update && s.corr == 2) k32_update<1, 2><<<grid1, kUT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
+            else if (update && s.corr) k32_update<1, 1><<<grid1, kUT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
+            else if (update) k32_update<1, 0><<<grid1, kUT, upd_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
             else k32_reconstruct<1><<<grid1, kT, tile_smem<1>(), stream>>>(s.d_inst, s.d_items, off1);
             ++n;
         }

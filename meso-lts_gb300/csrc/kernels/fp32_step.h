@@ -134,9 +134,6 @@ struct F32Inst {
     double *corrW;         // [C][4] rho, rho ux, rho uy, rho E after the conservative update
     double *corrq;         // [C][2] heat flux
     float2 *corrR;         // [C][NVp] on a measuring step: the rounding residual of each stored value
-    int *refine_pass;      // device flag: non-zero on a measuring step (the stored value rounded to
-                           // nearest and its residual kept, so the correction is measured without
-                           // the stochastic rounding's draw)
 };
 
 // Boundary faces of small velocity sets per boundary-kernel block (a warp each).
@@ -160,7 +157,8 @@ struct Fp32State {
     int has_small = 0, has_large = 0;  // instances with NVp <= / > F32_SMALL_NVP
     int total_faces = 0, total_cells = 0, total_bnd = 0;
     int num_sms = 0;
-    int corr = 0;                // the single instance carries defect corrections (corrS non-null)
+    int corr = 0;                // 1: the single instance carries defect corrections (corrS non-null);
+                                 // 2: this step measures them (the state rounded to nearest, residuals kept)
 };
 
 int fp32_configure(int device);
