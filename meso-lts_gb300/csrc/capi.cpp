@@ -209,6 +209,27 @@ int build_device(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d) {
             for (int k = 0; k < 3; ++k) sym[3 * p + k] = d->sym[3 * p + k];
     }
     c->nb = (int)bface.size();
+    // tensor-product velocity sets (2-D): every (x, y) of the distinct components present once
+    std::vector<double> tX, tY;
+    std::vector<int> tix(NV), tiy(NV);
+    if (D == 2) {
+        tX = xix;
+        tY = xiy;
+        std::sort(tX.begin(), tX.end());
+        tX.erase(std::unique(tX.begin(), tX.end()), tX.end());
+        std::sort(tY.begin(), tY.end());
+        tY.erase(std::unique(tY.begin(), tY.end()), tY.end());
+        bool tensor = tX.size() * tY.size() == (size_t)NV;
+        std::vector<char> seen(tensor ? (size_t)NV : 0, 0);
+        for (int p = 0; tensor && p < NV; ++p) {
+            tix[p] = (int)(std::lower_bound(tX.begin(), tX.end(), xix[p]) - tX.begin());
+            tiy[p] = (int)(std::lower_bound(tY.begin(), tY.end(), xiy[p]) - tY.begin());
+            char &c2 = seen[(size_t)tiy[p] * tX.size() + tix[p]];
+            tensor = !c2;
+            c2 = 1;
+        }
+        if (!tensor) tX.clear(), tY.clear();
+    }
     auto &A = c->arena;
     auto &dm = c->dm;
     dm.dim = D;
@@ -273,6 +294,20 @@ int build_device(meso_ctx *c, const meso_mesh_desc *m, const meso_dvs_desc *d) {
         dm.sym = p_sym;
         dm.marks = p_marks;
         dm.mask = p_mask;
+        if (!tX.empty()) {
+            double *p_tx = A.alloc<double>(tX.size()), *p_ty = A.alloc<double>(tY.size());
+            int *p_tix = A.alloc<int>(NV), *p_tiy = A.alloc<int>(NV);
+            upload(p_tx, tX, c->stream);
+            upload(p_ty, tY, c->stream);
+            upload(p_tix, tix, c->stream);
+            upload(p_tiy, tiy, c->stream);
+            dm.ntx = (int)tX.size();
+            dm.nty = (int)tY.size();
+            dm.tx = p_tx;
+            dm.ty = p_ty;
+            dm.tix = p_tix;
+            dm.tiy = p_tiy;
+        }
         c->d_status = A.alloc<meso::DStatus>(1);
 
         const bool shakhov = c->params.solver == MESO_SOLVER_CDUGKS_SHAKHOV;

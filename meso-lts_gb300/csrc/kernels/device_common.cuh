@@ -33,6 +33,11 @@ struct DMesh {
     const int *sym;         // [NV*3]
     const meso_mark_desc *marks;
     const uint8_t *mask;    // [C] cell mask switch (may be null)
+    // 2-D tensor-product velocity sets (NC, GH, hGH, D2Q9): xi_p = (tx[tix[p]], ty[tiy[p]]), so the
+    // Maxwellian's exponential factors into one per component; ntx = 0 for other sets
+    int ntx, nty;
+    const double *tx, *ty;
+    const int *tix, *tiy;
 };
 
 // Per-step scalars, derived on the host exactly as the reference derives them.

@@ -107,6 +107,22 @@ __device__ __forceinline__ void shakhov_eq(const KParams &k, const EqK64 &e, dou
     gs = (e.sg * cq) * (t - k.Dd - 2.0) * gm + gm;
     hs = (e.sh * cq) * ((t - k.Dd) * (k.Kd + 3.0 - k.Dd) - 2.0 * k.Kd) * gm + e.hm * gm;
 }
+// The same with the Maxwellian g_M given (tensor-product velocity sets: A e^(-cx^2/2RT) e^(-cy^2/2RT)).
+__device__ __forceinline__ void shakhov_eq_gm(const KParams &k, const EqK64 &e, double gm, double cc, double cq,
+                                              double &gs, double &hs) {
+    const double t = cc * e.iRT;
+    gs = (e.sg * cq) * (t - k.Dd - 2.0) * gm + gm;
+    hs = (e.sh * cq) * ((t - k.Dd) * (k.Kd + 3.0 - k.Dd) - 2.0 * k.Kd) * gm + e.hm * gm;
+}
+// The segment's factor tables at (u, 1/(2RT)): t[i] = e^(-(tx[i] - ux)^2 / 2RT) for i < ntx, then
+// e^(-(ty[j] - uy)^2 / 2RT); every lane of the segment takes part.
+__device__ __forceinline__ void exp_tables(const DMesh &m, V3 u, double oRT2, int lane, int L, double *t) {
+    for (int i = lane; i < m.ntx + m.nty; i += L) {
+        const double c = i < m.ntx ? m.tx[i] - u.x : m.ty[i - m.ntx] - u.y;
+        t[i] = exp(-(c * c) * oRT2);
+    }
+}
+
 template <int DIM> __device__ __forceinline__ double f_maxwell(const KParams &k, double rho, V3 u, V3 xi) {
     double ku_RT = dot<DIM>(u, xi) * k.over_RT;
     double uu_RT = dot<DIM>(u, u) * k.over_RT;
@@ -340,7 +356,6 @@ __global__ void __launch_bounds__(kBlock) k_face_eq(DMesh m, KParams k, const DS
             m3[2] += (c.z * w) * s;
         }
     seg_reduce<3>(m3, L, sh);
-    if (!active) return;
     const double rhoE = 0.5 * v[4];
     const V3 hu = scl(u, 0.5);
     const double T = (rhoE / rho - dot<DIM>(hu, u)) / k.Cv;
@@ -349,6 +364,24 @@ __global__ void __launch_bounds__(kBlock) k_face_eq(DMesh m, KParams k, const DS
     const V3 q = v3(m3[0] * qs, m3[1] * qs, m3[2] * qs);
     const double C_s = k.hdt / (2.0 * tau + k.hdt);
     const EqK64 e = make_eqk<DIM>(k, rho, T);
+    if (DIM == 2 && m.ntx > 0) {  // tensor-product set: the exponential from two factor tables
+        extern __shared__ double tabs[];
+        double *t = tabs + (threadIdx.x / L) * (m.ntx + m.nty);
+        exp_tables(m, u, e.oRT2, lane, L, t);
+        __syncthreads();  // every thread of the block gets here (inactive segments too)
+        if (!active) return;
+        for (int p = lane; p < m.NV; p += L) {
+            const V3 c = xi_of(m, p) - u;
+            const double cc = dot<DIM>(c, c);
+            const double cq = dot<DIM>(c, q);
+            double g_s, h_s;
+            shakhov_eq_gm(k, e, e.A * (t[m.tix[p]] * t[m.ntx + m.tiy[p]]), cc, cq, g_s, h_s);
+            face0[base + p] = (1.0 - C_s) * face0[base + p] + C_s * g_s;
+            face1[base + p] = (1.0 - C_s) * face1[base + p] + C_s * h_s;
+        }
+        return;
+    }
+    if (!active) return;
     for (int p = lane; p < m.NV; p += L) {
         const V3 c = xi_of(m, p) - u;
         const double cc = dot<DIM>(c, c);
@@ -622,6 +655,16 @@ __global__ void __launch_bounds__(kBlock) k_update_shakhov(DMesh m, KParams k, D
     const double C_s = k.hdt / (2.0 * tau);
     const double itau = 1.0 / tau, itau_n = 1.0 / tau_n;
     const EqK64 e_n = make_eqk<DIM>(k, rho_n, T_n), e1 = make_eqk<DIM>(k, rho, T);
+    // tensor-product set: the two equilibria's exponentials from factor tables (state n, then n+1)
+    const bool tensor = DIM == 2 && m.ntx > 0;
+    extern __shared__ double tabs[];
+    const int nt = m.ntx + m.nty;
+    double *tn = tabs + (threadIdx.x / L) * 2 * nt, *t1 = tn + nt;
+    if (tensor) {
+        exp_tables(m, u_n, e_n.oRT2, lane, L, tn);
+        exp_tables(m, u, e1.oRT2, lane, L, t1);
+        __syncthreads();  // every thread of the block gets here (inactive segments too)
+    }
     double m3[3] = {0, 0, 0};
     if (active)
         for (int p = lane; p < m.NV; p += L) {
@@ -630,14 +673,17 @@ __global__ void __launch_bounds__(kBlock) k_update_shakhov(DMesh m, KParams k, D
             const double cc_n = dot<DIM>(c_n, c_n);
             const double cq_n = dot<DIM>(c_n, q_n);
             double g_s_n, h_s_n;
-            shakhov_eq(k, e_n, cc_n, cq_n, g_s_n, h_s_n);
+            const int ix = tensor ? m.tix[p] : 0, iy = tensor ? m.ntx + m.tiy[p] : 0;
+            if (tensor) shakhov_eq_gm(k, e_n, e_n.A * (tn[ix] * tn[iy]), cc_n, cq_n, g_s_n, h_s_n);
+            else shakhov_eq(k, e_n, cc_n, cq_n, g_s_n, h_s_n);
             const double g_n = cm * g_s_n + (1.0 - cm) * g_cell[base + p];
             const double h_n = cm * h_s_n + (1.0 - cm) * h_cell[base + p];
             const V3 cv = xi - u;
             const double cc = dot<DIM>(cv, cv);
             const double cq = dot<DIM>(cv, q_n);
             double g_s, h_s;
-            shakhov_eq(k, e1, cc, cq, g_s, h_s);
+            if (tensor) shakhov_eq_gm(k, e1, e1.A * (t1[ix] * t1[iy]), cc, cq, g_s, h_s);
+            else shakhov_eq(k, e1, cc, cq, g_s, h_s);
             const double g = Cc * (g_n + k.hdt * (g_s * itau + (g_s_n - g_n) * itau_n) - dt_v * flux_g[base + p]);
             const double h = Cc * (h_n + k.hdt * (h_s * itau + (h_s_n - h_n) * itau_n) - dt_v * flux_h[base + p]);
             const double hw = 0.5 * m.w[p];
@@ -959,7 +1005,8 @@ int plain_step_dim(const PlainState &s, cudaStream_t stream, int64_t *launches, 
         k_recon<DIM, 2, true><<<grid_for(fv, sms), kBlock, 0, stream>>>(m, k, s.status, s.f0, s.f1, s.grad0, s.grad1,
                                                                          s.face0, s.face1);
         mark(2);
-        k_face_eq<DIM, true><<<(m.F + spb - 1) / spb, kBlock, 0, stream>>>(m, k, s.status, L, s.face0, s.face1);
+        const size_t tab = DIM == 2 && m.ntx > 0 ? sizeof(double) * (size_t)spb * (m.ntx + m.nty) : 0;
+        k_face_eq<DIM, true><<<(m.F + spb - 1) / spb, kBlock, tab, stream>>>(m, k, s.status, L, s.face0, s.face1);
         mark(3);
         n += 2;
         if (m.nb > 0) {
@@ -968,7 +1015,7 @@ int plain_step_dim(const PlainState &s, cudaStream_t stream, int64_t *launches, 
             ++n;
         }
         mark(4);
-        k_update_shakhov<DIM><<<(m.C + spb - 1) / spb, kBlock, 0, stream>>>(
+        k_update_shakhov<DIM><<<(m.C + spb - 1) / spb, kBlock, 2 * tab, stream>>>(
             m, k, s.status, L, s.f0, s.f1, s.face0, s.face1, s.flux0, s.flux1, s.rho, s.u, s.T, s.q, s.fm0, s.fm1,
             s.fm2, s.repair_list);
         k_mask_repair<DIM><<<64, kBlock, 0, stream>>>(m, k, s.status, s.repair_list, s.f0, s.f1, s.rho, s.u, s.T, s.q);
