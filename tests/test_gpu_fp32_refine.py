@@ -100,6 +100,21 @@ def test_refine_rules(gpu, tmp_path):
     with pytest.raises(mg.MesoError) as e:
         mg.Batch([s32])
     assert e.value.code == mg.ERR_UNSUPPORTED
+    # new settings keep the correction (the step constants reach the FP64 step too)
+    s32.step(4)
+    prm = s32.params
+    prm.dt = prm.dt * 0.5
+    s32.set_params(prm)
+    s32.step(8)
+    ref64 = _solver(case, mg.FP64, rho, u, T, mask)
+    ref64.step(4)
+    p64 = mg.Params.from_buffer_copy(prm)
+    p64.precision = mg.FP64
+    ref64.set_params(p64)
+    ref64.step(8)
+    e = _errs(s32.macros(case.ncell), ref64.macros(case.ncell))
+    assert e["rho"] <= 1e-7 and e["T"] <= 1e-7 and e["u"] <= 1e-5, e
+    ref64.close()
     # switched off, the solve steps as a plain FP32 solve again (and may join a batch)
     s32.refine(0)
     s32.step(8)
