@@ -3,9 +3,11 @@
 Usage: python meso-lts_gb300/build.py [--force]
 
 Host C++ is compiled with -ffp-contract=off so the geometry it builds matches
-the reference bit for bit on x86-64 and aarch64 alike; the plain FP64 kernels
-are compiled with -fmad=false for the same reason.  Objects are rebuilt when
-their source or any header in the tree is newer.
+the reference bit for bit on x86-64 and aarch64 alike.  The plain FP64 kernels
+are compiled twice: the 2-D ones with multiply-adds contracted (their parity
+gates hold at 1e-12 that way and the FP64 pipe bounds them), the 3-D ones with
+-fmad=false.  Objects are rebuilt when their source or any header in the tree
+is newer.
 """
 from __future__ import annotations
 
@@ -27,10 +29,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SRCS = ["host/mesh.cpp", "host/config.cpp", "host/case.cpp", "host/renumber.cpp", "host/output.cpp",
              "host/tiles.cpp", "host/fp32_host.cpp", "capi.cpp", "batch.cpp", "server.cpp", "autotune.cpp"]
-# (source, extra nvcc flags)
-CUDA_SRCS = [("kernels/plain_fp64.cu", ["-fmad=false"]),
-             ("kernels/fp32_step.cu", []),
-             ("kernels/moments_noalloc.cu", ["-fmad=false"])]
+# (source, extra nvcc flags, object name)
+CUDA_SRCS = [("kernels/plain_fp64.cu", ["-DMESO_PLAIN_DIM=2"], "plain_fp64_2d"),
+             ("kernels/plain_fp64.cu", ["-DMESO_PLAIN_DIM=3", "-fmad=false"], "plain_fp64_3d"),
+             ("kernels/fp32_step.cu", [], "fp32_step"),
+             ("kernels/moments_noalloc.cu", ["-fmad=false"], "moments_noalloc")]
 
 LIB = os.path.join(LIBDIR, "libmeso_gpu.so")
 ORACLE_LIB = os.path.join(ORACLE, "lib", "libmeso_oracle.so")
@@ -73,11 +76,11 @@ def build_library(force: bool = False, jobs: int | None = None) -> str:
         if force or _stale(src, obj, hdr_t):
             jobs_list.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
                               *inc, "-c", src, "-o", obj])
-    for s, extra in CUDA_SRCS:
+    for s, extra, name in CUDA_SRCS:
         src = os.path.join(CSRC, s)
         if not os.path.exists(src):
             continue
-        obj = os.path.join(OBJDIR, s.replace("/", "_") + ".o")
+        obj = os.path.join(OBJDIR, name + ".cu.o")
         objs.append(obj)
         if force or _stale(src, obj, hdr_t):
             jobs_list.append([nvcc, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",

@@ -1074,14 +1074,22 @@ int plain_init_dim(const PlainState &s, int mode, cudaStream_t stream) {
 
 }  // namespace
 
+// This file is compiled once per dimension (MESO_PLAIN_DIM): the 2-D kernels with multiply-adds
+// contracted, the 3-D ones with contraction off (see plain_fp64.h).
+#if MESO_PLAIN_DIM == 3
+int plain_step_d3(const PlainState &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev) {
+    return plain_step_dim<3>(s, stream, launches, ev);
+}
+int plain_init_d3(const PlainState &s, int mode, cudaStream_t stream) { return plain_init_dim<3>(s, mode, stream); }
+#elif MESO_PLAIN_DIM == 2
 const char *const kPlainPhases[] = {"k_grad", "k_recon", "k_face_eq", "k_boundary", "k_update+repair", "k_end_step"};
 
 int plain_step(const PlainState &s, cudaStream_t stream, int64_t *launches, cudaEvent_t *ev) {
-    return s.mesh.dim == 2 ? plain_step_dim<2>(s, stream, launches, ev) : plain_step_dim<3>(s, stream, launches, ev);
+    return s.mesh.dim == 2 ? plain_step_dim<2>(s, stream, launches, ev) : plain_step_d3(s, stream, launches, ev);
 }
 
 int plain_init(const PlainState &s, int mode, cudaStream_t stream) {
-    return s.mesh.dim == 2 ? plain_init_dim<2>(s, mode, stream) : plain_init_dim<3>(s, mode, stream);
+    return s.mesh.dim == 2 ? plain_init_dim<2>(s, mode, stream) : plain_init_d3(s, mode, stream);
 }
 
 int gather_macros(const double *rho, const double *u, const double *T, const double *q, const int *new2old, int C,
@@ -1089,5 +1097,8 @@ int gather_macros(const double *rho, const double *u, const double *T, const dou
     k_gather_macros<<<grid_for((size_t)C, sms), kBlock, 0, stream>>>(rho, u, T, q, new2old, C, out);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
+#else
+#error "plain_fp64.cu is compiled with -DMESO_PLAIN_DIM=2 or -DMESO_PLAIN_DIM=3"
+#endif
 
 }  // namespace meso
