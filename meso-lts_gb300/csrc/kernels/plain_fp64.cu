@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(kBlock) k_face_eq(DMesh m, KParams k, const DS
                 const double wf = w * f;
                 v[1] += xi.x * wf;
                 v[2] += xi.y * wf;
-                v[3] += xi.z * wf;
+                if (DIM == 3) v[3] += xi.z * wf;
             }
         seg_reduce<4>(v, L, sh);
         if (!active) return;
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(kBlock) k_face_eq(DMesh m, KParams k, const DS
             const double wg = w * g;
             v[1] += xi.x * wg;
             v[2] += xi.y * wg;
-            v[3] += xi.z * wg;
+            if (DIM == 3) v[3] += xi.z * wg;
             v[4] += w * (kk * g + h);
         }
     seg_reduce<5>(v, L, sh);
@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(kBlock) k_face_eq(DMesh m, KParams k, const DS
             const double s = cc * g + h;
             m3[0] += (c.x * w) * s;
             m3[1] += (c.y * w) * s;
-            m3[2] += (c.z * w) * s;
+            if (DIM == 3) m3[2] += (c.z * w) * s;
         }
     seg_reduce<3>(m3, L, sh);
     const double rhoE = 0.5 * v[4];
@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(kBlock) k_update_shakhov(DMesh m, KParams k, D
             const double wf = w * fg;
             v[1] += xi.x * wf;
             v[2] += xi.y * wf;
-            v[3] += xi.z * wf;
+            if (DIM == 3) v[3] += xi.z * wf;
             v[4] += w * (dot<DIM>(xi, xi) * fg + fh);
         }
     seg_reduce<5>(v, L, sh);
@@ -690,7 +690,7 @@ __global__ void __launch_bounds__(kBlock) k_update_shakhov(DMesh m, KParams k, D
             const double s = cc * g + h;
             m3[0] += (cv.x * hw) * s;
             m3[1] += (cv.y * hw) * s;
-            m3[2] += (cv.z * hw) * s;
+            if (DIM == 3) m3[2] += (cv.z * hw) * s;
             g_cell[base + p] = (1.0 - C_s) * g + C_s * g_s;
             h_cell[base + p] = (1.0 - C_s) * h + C_s * h_s;
         }
@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(kBlock) k_update_cdugks(DMesh m, KParams k, co
             const double wf = w * fl;
             v[1] += xi.x * wf;
             v[2] += xi.y * wf;
-            v[3] += xi.z * wf;
+            if (DIM == 3) v[3] += xi.z * wf;
         }
     seg_reduce<4>(v, L, sh);
     const int cc_ = active ? c : 0;
@@ -802,7 +802,7 @@ __global__ void __launch_bounds__(kBlock) k_update_dugks(DMesh m, KParams k, con
             const double wf = w * f;
             v[1] += xi.x * wf;
             v[2] += xi.y * wf;
-            v[3] += xi.z * wf;
+            if (DIM == 3) v[3] += xi.z * wf;
         }
     seg_reduce<4>(v, L, sh);
     const double rho = v[0];
@@ -847,7 +847,7 @@ __global__ void __launch_bounds__(kBlock) k_init(DMesh m, KParams k, int L, int 
                 const double wf = w * f;
                 v[1] += xi.x * wf;
                 v[2] += xi.y * wf;
-                v[3] += xi.z * wf;
+                if (DIM == 3) v[3] += xi.z * wf;
             }
         seg_reduce<8>(v, L, sh);
         if (!active || lane != 0 || mode != 0) return;
@@ -881,12 +881,12 @@ __global__ void __launch_bounds__(kBlock) k_init(DMesh m, KParams k, int L, int 
             const double wg = w * g;
             v[1] += xi.x * wg;
             v[2] += xi.y * wg;
-            v[3] += xi.z * wg;
+            if (DIM == 3) v[3] += xi.z * wg;
             v[4] += w * (kk * g + h);
             const double s = cc * g + h;
             v[5] += (c.x * w) * s;
             v[6] += (c.y * w) * s;
-            v[7] += (c.z * w) * s;
+            if (DIM == 3) v[7] += (c.z * w) * s;
         }
     seg_reduce<8>(v, L, sh);
     if (!active || lane != 0 || mode != 0) return;
